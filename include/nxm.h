@@ -1,0 +1,184 @@
+/*
+ * nexusmd-gb300: C ABI of the CUDA force-and-integrate engine (libnxm_cuda.so).
+ *
+ * Plain C types only: pointers, sizes, doubles.  Every function returns
+ * NXM_OK (0) or a negative NXM_ERR_* code; the message of the last failure
+ * is nxm_last_error() (thread-local).  Positions, velocities and forces are
+ * AoS double[n][3] in nm, nm/ps and kJ/mol/nm, the layout of the reference's
+ * std::vector<Coords3D> (core/common/headers/Coords3D.h:15-152).  Host
+ * buffers are owned by the caller; device memory is owned by the context.
+ * One CUDA stream per context; calls are synchronous with respect to the
+ * host buffers they take or fill.
+ *
+ * Reference interfaces each group replaces (paths in the NexusMD project):
+ *   nxm_dispatcher_*   TaskDispatcher / BaseLineTaskDispatcher
+ *                      (core/dispatcher/headers/TaskDispatcher.h:9-43,
+ *                       core/dispatcher/headers/BaseLineTaskDispatcher.h:9-52,
+ *                       core/dispatcher/src/TaskDispatcher.cpp:6-23), the
+ *                      object the SWIG module exposes (wrapper/NexusMD.i:1-19)
+ *   nxm_parse_*        SystemXMLParser / StateXMLParser
+ *                      (core/common/headers/SystemXMLParser.h:10-64,
+ *                       core/common/headers/StateXMLParser.h:9-18)
+ *   nxm_create .. nxm_destroy   BaseLine::Engine and its step loop
+ *                      (core/baseline/headers/Engine.h:25-93,
+ *                       core/baseline/src/Engine.cpp:75-188)
+ */
+#ifndef NXM_H
+#define NXM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NXM_OK 0
+#define NXM_ERR_INVALID -1   /* bad argument or inconsistent system */
+#define NXM_ERR_CUDA -2      /* CUDA runtime failure or no device */
+#define NXM_ERR_CAPACITY -3  /* neighbour list or exclusion capacity exceeded */
+#define NXM_ERR_NUMERIC -4   /* non-finite force */
+#define NXM_ERR_IO -5        /* file could not be read or written */
+
+#define NXM_FORCE_BOND 1
+#define NXM_FORCE_ANGLE 2
+#define NXM_FORCE_TORSION 4
+#define NXM_FORCE_NONBONDED 8
+
+#define NXM_PRECISION_FP64 0  /* FP64 everywhere, FP64 atomics */
+#define NXM_PRECISION_MIXED 1 /* FP32 forces, int64 fixed-point sums, FP64 x/v/energies */
+
+/* One system.  Index arrays are 0-based atom indices of this system. */
+typedef struct {
+    int32_t n_atoms;
+    const double *masses;   /* [n] */
+    const double *charges;  /* [n] e */
+    const double *sigmas;   /* [n] nm */
+    const double *epsilons; /* [n] kJ/mol */
+    int32_t n_bonds;
+    const int32_t *bond_atoms;  /* [n_bonds][2] */
+    const double *bond_params;  /* [n_bonds][2]: d (nm), k (kJ/mol/nm^2) */
+    int32_t n_angles;
+    const int32_t *angle_atoms; /* [n_angles][3] */
+    const double *angle_params; /* [n_angles][2]: a (rad), k (kJ/mol/rad^2) */
+    int32_t n_torsions;
+    const int32_t *torsion_atoms;       /* [n_torsions][4] */
+    const double *torsion_params;       /* [n_torsions][2]: k (kJ/mol), phase (rad) */
+    const int32_t *torsion_periodicity; /* [n_torsions] */
+    double cutoff;            /* nm */
+    double ewald_tolerance;   /* alpha = sqrt(-ln(2 tol)) / cutoff */
+    int32_t use_switching;    /* LJ switching function on/off */
+    double switching_distance;
+    int32_t grid[3];          /* PME grid; 0,0,0 = the reference's power-of-two rule */
+    int32_t box_from_positions; /* 1: atom extent + 1% per side, as the reference */
+    double box_lb[3], box_ub[3];  /* used when box_from_positions == 0 */
+    int32_t force_mask;       /* NXM_FORCE_* bits */
+    int32_t exclusion_depth;  /* bonds within which pairs are excluded; 3 in the reference */
+} nxm_system_desc;
+
+typedef struct {
+    int32_t precision;        /* NXM_PRECISION_* */
+    double skin;              /* nm; list radius = cutoff + skin */
+    int32_t rebuild_interval; /* max steps between list rebuilds (also rebuilt when an
+                                 atom moves more than skin/2); 1 = every step */
+    int32_t device;           /* CUDA device ordinal */
+    int32_t max_neighbors;    /* list capacity per atom; 0 = from density */
+} nxm_options;
+
+/* Energies of one system (kJ/mol) at the last evaluation that computed them. */
+typedef struct {
+    double bond, angle, torsion;
+    double recip, self, coulomb, vdw, exclusion; /* PE(nonbonded) = recip+self+coulomb+vdw-exclusion */
+    double kinetic;
+    double potential;          /* sum of the enabled terms */
+    double reported_potential; /* the reference's TotalEnergy value: reciprocal energy
+                                  replaces the bonded sum when nonbonded is on
+                                  (NonbondedForce.cpp:387) */
+} nxm_energies;
+
+typedef struct nxm_ctx nxm_ctx;
+
+const char *nxm_version(void);
+const char *nxm_last_error(void);
+void nxm_default_options(nxm_options *opt);
+
+/* Create a context for n_systems systems; positions = all systems' atoms
+ * concatenated [sum n][3].  Velocities start at zero (Initializer.cpp:18-24). */
+int nxm_create(const nxm_system_desc *systems, int32_t n_systems, const nxm_options *opt,
+               const double *positions, nxm_ctx **out);
+void nxm_destroy(nxm_ctx *ctx);
+
+int nxm_n_atoms(const nxm_ctx *ctx, int32_t *n_total);
+int nxm_set_positions(nxm_ctx *ctx, const double *xyz);
+int nxm_set_velocities(nxm_ctx *ctx, const double *xyz);
+
+/* Forces and energies at the current positions (no integration). */
+int nxm_compute_forces(nxm_ctx *ctx);
+
+/* nsteps leapfrog steps of dt ps.  Energies and the x/v/F snapshot are taken
+ * on the last step (and the kinetic energy with them). */
+int nxm_step(nxm_ctx *ctx, int32_t nsteps, double dt);
+
+/* Snapshot of the last force evaluation: positions and velocities as they
+ * were when the forces were computed (before that step's update). */
+int nxm_get_positions(nxm_ctx *ctx, double *xyz);
+int nxm_get_velocities(nxm_ctx *ctx, double *xyz);
+int nxm_get_forces(nxm_ctx *ctx, double *xyz);
+/* Positions/velocities now (after the last update). */
+int nxm_get_state(nxm_ctx *ctx, double *xyz, double *vel);
+int nxm_get_energies(nxm_ctx *ctx, int32_t system, nxm_energies *out);
+int nxm_get_box(nxm_ctx *ctx, int32_t system, double lb[3], double ub[3]);
+int nxm_get_grid(nxm_ctx *ctx, int32_t system, int32_t grid[3]);
+int nxm_get_alpha(nxm_ctx *ctx, int32_t system, double *alpha);
+
+/* Neighbour pair set of one system within the cutoff at the current
+ * positions, as the reference's list decides it (NeighborList.cpp:129-154):
+ * pairs (i, j), i > j, this system's atom indices, in no particular order.
+ * Returns the pair count (>= 0; only min(count, cap) pairs written) or an
+ * error code. */
+int64_t nxm_get_pairs(nxm_ctx *ctx, int32_t system, int32_t *pairs, int64_t cap);
+
+/* Time one call of nxm_step(nsteps) on the device (CUDA events on the
+ * context's stream, after the call's launches); milliseconds. */
+int nxm_time_steps(nxm_ctx *ctx, int32_t nsteps, double dt, double *ms);
+
+/* Kernel launches one step issues (steady state, no list rebuild). */
+int nxm_launches_per_step(nxm_ctx *ctx, int32_t *launches, int32_t *rebuild_launches);
+
+/* ---- SystemXMLParser / StateXMLParser (SystemXMLParser.cpp:18-196,
+ * StateXMLParser.cpp:17-59).  A parsed system is owned by the library. */
+typedef struct nxm_parsed nxm_parsed;
+int nxm_parse_files(const char *system_xml, const char *state_xml, nxm_parsed **out);
+void nxm_parsed_free(nxm_parsed *p);
+/* Counts: atoms (masses), positions, bonds, angles, torsions, nonbonded particles, exceptions. */
+int nxm_parsed_counts(const nxm_parsed *p, int64_t counts[7]);
+/* Nonbonded scalars: cutoff, ewaldTolerance, switchingDistance, useSwitchingFunction,
+ * alpha, rfDielectric, nx, ny, nz, method, dispersionCorrection. */
+int nxm_parsed_nonbonded(const nxm_parsed *p, double out[11]);
+/* Fill caller arrays (any pointer may be NULL to skip). */
+int nxm_parsed_arrays(const nxm_parsed *p, double *masses, double *positions, int32_t *bond_atoms,
+                      double *bond_params, int32_t *angle_atoms, double *angle_params,
+                      int32_t *torsion_atoms, double *torsion_params, int32_t *torsion_per,
+                      double *q_sig_eps, int32_t *exception_atoms, double *exception_params);
+
+/* ---- TaskDispatcher (TaskDispatcher.h:9-43).  "GPU" / "CUDA" select the
+ * CUDA engine; any other string prints the reference's complaint and also
+ * selects it (this library has no CPU engine). */
+typedef struct nxm_dispatcher nxm_dispatcher;
+int nxm_dispatcher_create(const char *processor, nxm_dispatcher **out);
+void nxm_dispatcher_destroy(nxm_dispatcher *d);
+int nxm_dispatcher_enable_harmonic_bond_force(nxm_dispatcher *d);
+int nxm_dispatcher_enable_harmonic_angle_force(nxm_dispatcher *d);
+int nxm_dispatcher_enable_periodic_torsion_force(nxm_dispatcher *d);
+int nxm_dispatcher_enable_nonbonded_force(nxm_dispatcher *d);
+/* Engine options the reference hard-codes (precision, list skin, grid). */
+int nxm_dispatcher_set_options(nxm_dispatcher *d, const nxm_options *opt);
+/* TaskDispatcher::Simulate (BaseLineTaskDispatcher.h:12-40, Engine.cpp:162-188):
+ * writes PVFReport<out>, TotalEnergy<out> and <out> in the reference's formats. */
+int nxm_dispatcher_simulate(nxm_dispatcher *d, const char *system_xml, const char *state_xml,
+                            const char *input_pdb, const char *output_pdb, double step_size,
+                            int32_t total_steps, int32_t interval);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NXM_H */

@@ -1,0 +1,137 @@
+// Leapfrog update, kinetic energy and report snapshot, one thread per slot.
+//
+// VerletIntegration::Advance (core/baseline/src/VerletIntegration.cpp:49-89)
+// with dt[0] = dt[1] = dt: v += invm F dt; x' = x + v dt; one +-L wrap into
+// [lb, ub]; atoms with invm == 0 stay put.  On report steps the kinetic
+// energy of the on-step velocity estimate v + F dt / (2m)
+// (KineticEnergy.cpp:21-41) and a copy of x, v, F in original atom order are
+// taken before the update, which is where Engine::Report sits
+// (Engine.cpp:162-188).  The force accumulators are read, converted to FP64
+// and cleared here, so the next step starts from zero without a memset.
+#include "nxm_view.h"
+
+namespace nxm {
+
+template <typename Acc>
+__global__ void __launch_bounds__(256) k_integrate(DevView v, double dt, int report) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    bool live = s < v.N;
+    int sys = live ? v.sys_of[s] : 0;
+    double ke = 0.0;
+    if (live) {
+        const SysDev &S = v.sys[sys];
+        Acc *ax = static_cast<Acc *>(v.fx) + s;
+        Acc *ay = static_cast<Acc *>(v.fy) + s;
+        Acc *az = static_cast<Acc *>(v.fz) + s;
+        double F[3] = {acc_value(*ax), acc_value(*ay), acc_value(*az)};
+        *ax = (Acc)0;
+        *ay = (Acc)0;
+        *az = (Acc)0;
+        double p[3] = {v.x[s], v.y[s], v.z[s]};
+        double u[3] = {v.vx[s], v.vy[s], v.vz[s]};
+        if (report) {
+            int o = v.orig[s];
+            double m = v.mass[s];
+            double w[3] = {u[0], u[1], u[2]};
+            if (m > 0) {
+                double invMass = 1.0 / m;
+                double half = 0.5 * dt;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) w[c] += F[c] * invMass * half;
+            }
+            ke = 0.5 * m * (w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                v.snap_x[3 * (size_t)o + c] = p[c];
+                v.snap_v[3 * (size_t)o + c] = u[c];
+                v.snap_f[3 * (size_t)o + c] = F[c];
+            }
+        }
+        double im = v.invm[s];
+        if (im != 0.0) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                u[c] += im * F[c] * dt;
+                double q = p[c] + u[c] * dt;
+                if (q < S.lb[c])
+                    q += S.L[c];
+                else if (q > S.ub[c])
+                    q -= S.L[c];
+                p[c] = q;
+            }
+            v.x[s] = p[0];
+            v.y[s] = p[1];
+            v.z[s] = p[2];
+            v.vx[s] = u[0];
+            v.vy[s] = u[1];
+            v.vz[s] = u[2];
+        }
+        if (v.mixed) {
+            int c3 = v.cell3[s];
+            int ci[3] = {c3 & 1023, (c3 >> 10) & 1023, (c3 >> 20) & 1023};
+            float o[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                o[c] = (float)min_image(p[c] - (S.lb[c] + ci[c] * S.cs[c]), S.L[c], S.halfL[c]);
+            float4 pf = v.pf[s];
+            v.pf[s] = make_float4(o[0], o[1], o[2], pf.w);
+        }
+        if (v.skin_half2 > 0.0) {
+            double d2 = 0.0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                double d = min_image(p[c] - v.xref[(size_t)c * v.N + s], S.L[c], S.halfL[c]);
+                d2 += d * d;
+            }
+            if (d2 > v.skin_half2) atomicOr(&v.flags->skin_hit, 1);
+        }
+        if (!(isfinite(F[0]) && isfinite(F[1]) && isfinite(F[2]))) atomicOr(&v.flags->error, ERR_NONFINITE);
+    }
+    if (report) energy_add(v.E, sys, E_KIN, ke);
+}
+
+// Copy positions, velocities and (optionally) the accumulated forces to the
+// original-order snapshot; forces are cleared after the copy.
+template <typename Acc>
+__global__ void k_export(DevView v, int with_forces) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= v.N) return;
+    int o = v.orig[s];
+    v.snap_x[3 * (size_t)o] = v.x[s];
+    v.snap_x[3 * (size_t)o + 1] = v.y[s];
+    v.snap_x[3 * (size_t)o + 2] = v.z[s];
+    v.snap_v[3 * (size_t)o] = v.vx[s];
+    v.snap_v[3 * (size_t)o + 1] = v.vy[s];
+    v.snap_v[3 * (size_t)o + 2] = v.vz[s];
+    if (with_forces) {
+        Acc *ax = static_cast<Acc *>(v.fx) + s;
+        Acc *ay = static_cast<Acc *>(v.fy) + s;
+        Acc *az = static_cast<Acc *>(v.fz) + s;
+        v.snap_f[3 * (size_t)o] = acc_value(*ax);
+        v.snap_f[3 * (size_t)o + 1] = acc_value(*ay);
+        v.snap_f[3 * (size_t)o + 2] = acc_value(*az);
+        *ax = (Acc)0;
+        *ay = (Acc)0;
+        *az = (Acc)0;
+    }
+}
+
+void launch_integrate(const DevView &v, double dt, int report, cudaStream_t st) {
+    int nb = (v.N + 255) / 256;
+    if (v.mixed)
+        k_integrate<long long><<<nb, 256, 0, st>>>(v, dt, report);
+    else
+        k_integrate<double><<<nb, 256, 0, st>>>(v, dt, report);
+}
+
+void launch_export(const DevView &v, int with_forces, cudaStream_t st) {
+    int nb = (v.N + 255) / 256;
+    if (v.mixed)
+        k_export<long long><<<nb, 256, 0, st>>>(v, with_forces);
+    else
+        k_export<double><<<nb, 256, 0, st>>>(v, with_forces);
+}
+
+void launch_snapshot_forces(const DevView &v, cudaStream_t st) { launch_export(v, 1, st); }
+
+}  // namespace nxm

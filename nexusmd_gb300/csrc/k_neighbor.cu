@@ -1,0 +1,335 @@
+// Neighbour-list rebuild: cell binning, a deterministic spatial sort of the
+// slots, permutation of the per-atom state, and a full (both directions)
+// per-atom Verlet list built one warp per atom with ballot compaction.
+//
+// Replaces the reference's per-step std::map voxel hash
+// (core/baseline/src/Forces/NeighborList.cpp:12-154).  The set of pairs that
+// reach the force kernels is the reference's: every non-excluded pair whose
+// single-shift minimum-image r^2 (FP64, PeriodicBoundaryCondition.cpp:93-104)
+// is below cutoff^2; the list holds a superset (cutoff + skin, with an FP32
+// safety margin) and the exact test is made per step in the pair kernels.
+#include "nxm_view.h"
+
+namespace nxm {
+
+__device__ __forceinline__ int wrapi(int a, int n) {
+    a %= n;
+    return a < 0 ? a + n : a;
+}
+
+__device__ __forceinline__ void cell_of(const SysDev &S, double x, double y, double z, int c[3]) {
+    double p[3] = {x, y, z};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        double u = (p[d] - S.lb[d]) * S.invL[d];
+        u -= floor(u);
+        int k = (int)(u * S.nc[d]);
+        c[d] = k < 0 ? 0 : (k >= S.nc[d] ? S.nc[d] - 1 : k);
+    }
+}
+
+__global__ void k_zero_cells(DevView v) {
+    if (!v.flags->rebuild) return;
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < v.total_cells) {
+        v.cell_count[c] = 0;
+        v.cell_fill[c] = 0;
+    }
+}
+
+__global__ void k_assign(DevView v) {
+    if (!v.flags->rebuild) return;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= v.N) return;
+    const SysDev &S = v.sys[v.sys_of[s]];
+    int c[3];
+    cell_of(S, v.x[s], v.y[s], v.z[s], c);
+    int key = S.cell_off + (c[0] * S.nc[1] + c[1]) * S.nc[2] + c[2];
+    v.cell_key[s] = key;
+    atomicAdd(&v.cell_count[key], 1);
+}
+
+// Exclusive scan of n ints by one block; out[n] = total.
+__global__ void k_scan(const Flags *flags, const int *in, int *out, int n) {
+    if (!flags->rebuild) return;
+    __shared__ int wsum[32];
+    __shared__ int carry;
+    const unsigned full = 0xffffffffu;
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < n; base += blockDim.x) {
+        int i = base + threadIdx.x;
+        int val = i < n ? in[i] : 0;
+        int xs = val;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(full, xs, o);
+            if (lane >= o) xs += y;
+        }
+        if (lane == 31) wsum[w] = xs;
+        __syncthreads();
+        if (w == 0) {
+            int ws = lane < nw ? wsum[lane] : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(full, ws, o);
+                if (lane >= o) ws += y;
+            }
+            wsum[lane] = ws;
+        }
+        __syncthreads();
+        int prefix = carry + (w > 0 ? wsum[w - 1] : 0) + xs - val;
+        if (i < n) out[i] = prefix;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = prefix + val;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[n] = carry;
+}
+
+__global__ void k_scatter(DevView v) {
+    if (!v.flags->rebuild) return;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= v.N) return;
+    int key = v.cell_key[s];
+    int pos = atomicAdd(&v.cell_fill[key], 1);
+    v.new_orig[v.cell_start[key] + pos] = v.orig[s];
+}
+
+// Order inside a cell by original index, so the layout (and every sum that
+// follows it) does not depend on atomic arrival order.
+__global__ void k_cellsort(DevView v) {
+    if (!v.flags->rebuild) return;
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= v.total_cells) return;
+    int a = v.cell_start[c], b = v.cell_start[c + 1];
+    for (int i = a + 1; i < b; ++i) {
+        int key = v.new_orig[i];
+        int j = i - 1;
+        while (j >= a && v.new_orig[j] > key) {
+            v.new_orig[j + 1] = v.new_orig[j];
+            --j;
+        }
+        v.new_orig[j + 1] = key;
+    }
+}
+
+constexpr int kPermArrays = 11;
+
+__global__ void k_permute_gather(DevView v) {
+    if (!v.flags->rebuild) return;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= v.N) return;
+    int so = v.slot_of[v.new_orig[s]];
+    const double *src[kPermArrays] = {v.x, v.y, v.z, v.vx, v.vy, v.vz, v.mass, v.invm, v.q, v.sig, v.eps};
+#pragma unroll
+    for (int k = 0; k < kPermArrays; ++k) v.tmp[(size_t)k * v.N + s] = src[k][so];
+}
+
+__global__ void k_permute_scatter(DevView v) {
+    if (!v.flags->rebuild) return;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= v.N) return;
+    double *dst[kPermArrays] = {v.x, v.y, v.z, v.vx, v.vy, v.vz, v.mass, v.invm, v.q, v.sig, v.eps};
+#pragma unroll
+    for (int k = 0; k < kPermArrays; ++k) dst[k][s] = v.tmp[(size_t)k * v.N + s];
+    int o = v.new_orig[s];
+    v.orig[s] = o;
+    v.slot_of[o] = s;
+}
+
+// Per-slot derived inputs: cell coordinates, cell-relative FP32 offsets,
+// scaled charges and combined LJ parameters (NonbondedForce.cpp:504-513:
+// sigma/2 and 2 sqrt(eps)), and the rebuild-time reference positions.
+__global__ void k_derive(DevView v, int gated) {
+    if (gated && !v.flags->rebuild) return;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= v.N) return;
+    const SysDev &S = v.sys[v.sys_of[s]];
+    double x = v.x[s], y = v.y[s], z = v.z[s];
+    int c[3];
+    cell_of(S, x, y, z, c);
+    v.cell3[s] = c[0] | (c[1] << 10) | (c[2] << 20);
+    double qs = v.q[s] * sqrt(kOne4PiEps0);
+    double sg = 0.5 * v.sig[s];
+    double ep = 2.0 * sqrt(v.eps[s]);
+    if (v.mixed) {
+        double p[3] = {x, y, z};
+        float o[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            double org = S.lb[d] + c[d] * S.cs[d];
+            o[d] = (float)min_image(p[d] - org, S.L[d], S.halfL[d]);
+        }
+        v.pf[s] = make_float4(o[0], o[1], o[2], (float)qs);
+        v.ljf[s] = make_float2((float)sg, (float)ep);
+    } else {
+        v.qs[s] = qs;
+        v.ljd[s] = make_double2(sg, ep);
+    }
+    v.xref[s] = x;
+    v.xref[v.N + s] = y;
+    v.xref[2 * v.N + s] = z;
+}
+
+// One warp per atom i: scan the 5x5x5 block of cells around i's cell (cells
+// are >= (cutoff + skin)/2 wide), skipping cells whose box is farther than
+// the list radius from i, and append every j != i within the list radius
+// that is not in i's exclusion set.  Entry = slot j | (cell-image code << 25);
+// dtab[code] is the FP32 displacement that turns j's cell-relative offset
+// into i's frame, so the pair kernel needs no minimum-image arithmetic.
+__global__ void __launch_bounds__(256) k_build(DevView v) {
+    const unsigned full = 0xffffffffu;
+    if (!v.flags->rebuild) return;
+    int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (i >= v.N) return;
+    int sys = v.sys_of[i];
+    const SysDev &S = v.sys[sys];
+    if (!S.nb_on) {
+        if (lane == 0) v.ncount[i] = 0;
+        return;
+    }
+    int c3 = v.cell3[i];
+    int ci[3] = {c3 & 1023, (c3 >> 10) & 1023, (c3 >> 20) & 1023};
+    float pix, piy, piz;
+    if (v.mixed) {
+        float4 p = v.pf[i];
+        pix = p.x;
+        piy = p.y;
+        piz = p.z;
+    } else {
+        double px = v.x[i], py = v.y[i], pz = v.z[i];
+        pix = (float)min_image(px - (S.lb[0] + ci[0] * S.cs[0]), S.L[0], S.halfL[0]);
+        piy = (float)min_image(py - (S.lb[1] + ci[1] * S.cs[1]), S.L[1], S.halfL[1]);
+        piz = (float)min_image(pz - (S.lb[2] + ci[2] * S.cs[2]), S.L[2], S.halfL[2]);
+    }
+    float pi3[3] = {pix, piy, piz};
+    float csf[3] = {(float)S.cs[0], (float)S.cs[1], (float)S.cs[2]};
+    int oi = v.orig[i];
+    int e0 = v.excl_off[oi];
+    int ne = v.excl_off[oi + 1] - e0;
+    int my_ex = lane < ne ? v.excl_lst[e0 + lane] : -1;
+    int nfast = ne < 32 ? ne : 32;
+    // FP32 positions of the list test carry ~1e-7 nm error; the margin keeps
+    // every pair the exact FP64 test could accept.
+    float rl2 = S.rlist2f * 1.0001f + 1e-6f;
+    int count = 0;
+    size_t base = (size_t)i * v.stride;
+    for (int ox = -2; ox <= 2; ++ox) {
+        float gx = ox > 0 ? ox * csf[0] - pi3[0] : (ox < 0 ? pi3[0] - (ox + 1) * csf[0] : 0.f);
+        gx = fmaxf(gx, 0.f);
+        int nx = wrapi(ci[0] + ox, S.nc[0]);
+        for (int oy = -2; oy <= 2; ++oy) {
+            float gy = oy > 0 ? oy * csf[1] - pi3[1] : (oy < 0 ? pi3[1] - (oy + 1) * csf[1] : 0.f);
+            gy = fmaxf(gy, 0.f);
+            int ny = wrapi(ci[1] + oy, S.nc[1]);
+            for (int oz = -2; oz <= 2; ++oz) {
+                float gz = oz > 0 ? oz * csf[2] - pi3[2] : (oz < 0 ? pi3[2] - (oz + 1) * csf[2] : 0.f);
+                gz = fmaxf(gz, 0.f);
+                if (gx * gx + gy * gy + gz * gz > rl2) continue;  // uniform across the warp
+                int nz = wrapi(ci[2] + oz, S.nc[2]);
+                int code = (ox + 2) * 25 + (oy + 2) * 5 + (oz + 2);
+                float4 D = v.dtab[sys * 128 + code];
+                int key = S.cell_off + (nx * S.nc[1] + ny) * S.nc[2] + nz;
+                int a = v.cell_start[key], b = v.cell_start[key + 1];
+                for (int j0 = a; j0 < b; j0 += 32) {
+                    int j = j0 + lane;
+                    bool cand = false;
+                    if (j < b && j != i) {
+                        float dx, dy, dz;
+                        if (v.mixed) {
+                            float4 pj = v.pf[j];
+                            dx = pix - pj.x + D.x;
+                            dy = piy - pj.y + D.y;
+                            dz = piz - pj.z + D.z;
+                        } else {
+                            int cj = v.cell3[j];
+                            int cjx = cj & 1023, cjy = (cj >> 10) & 1023, cjz = (cj >> 20) & 1023;
+                            float qx = (float)min_image(v.x[j] - (S.lb[0] + cjx * S.cs[0]), S.L[0], S.halfL[0]);
+                            float qy = (float)min_image(v.y[j] - (S.lb[1] + cjy * S.cs[1]), S.L[1], S.halfL[1]);
+                            float qz = (float)min_image(v.z[j] - (S.lb[2] + cjz * S.cs[2]), S.L[2], S.halfL[2]);
+                            dx = pix - qx + D.x;
+                            dy = piy - qy + D.y;
+                            dz = piz - qz + D.z;
+                        }
+                        float r2 = dx * dx + dy * dy + dz * dz;
+                        cand = r2 < rl2;
+                    }
+                    if (!__any_sync(full, cand)) continue;
+                    int oj = cand ? v.orig[j] : -2;
+                    bool ex = false;
+                    for (int e = 0; e < nfast; ++e) ex |= (__shfl_sync(full, my_ex, e) == oj);
+                    if (ne > 32 && cand)
+                        for (int e = 32; e < ne; ++e) ex |= (v.excl_lst[e0 + e] == oj);
+                    bool ok = cand && !ex;
+                    unsigned m = __ballot_sync(full, ok);
+                    if (ok) {
+                        int pos = count + __popc(m & ((1u << lane) - 1u));
+                        if (pos < v.stride) v.nlist[base + pos] = (uint32_t)j | ((uint32_t)code << 25);
+                    }
+                    count += __popc(m);
+                }
+            }
+        }
+    }
+    if (lane == 0) {
+        v.ncount[i] = count < v.stride ? count : v.stride;
+        if (count > v.stride) atomicOr(&v.flags->error, ERR_NLIST_OVERFLOW);
+    }
+}
+
+__global__ void k_remap(DevView v) {
+    if (!v.flags->rebuild) return;
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < v.nb) {
+        int2 b = v.bond_orig[t];
+        v.bond_slot[t] = make_int2(v.slot_of[b.x], v.slot_of[b.y]);
+        return;
+    }
+    t -= v.nb;
+    if (t < v.na) {
+        int4 a = v.angle_orig[t];
+        v.angle_slot[t] = make_int4(v.slot_of[a.x], v.slot_of[a.y], v.slot_of[a.z], 0);
+        return;
+    }
+    t -= v.na;
+    if (t < v.nt) {
+        int4 a = v.tors_orig[t];
+        v.tors_slot[t] = make_int4(v.slot_of[a.x], v.slot_of[a.y], v.slot_of[a.z], v.slot_of[a.w]);
+        return;
+    }
+    t -= v.nt;
+    if (t < v.nex) {
+        int2 e = v.ex_orig[t];
+        v.ex_slot[t] = make_int2(v.slot_of[e.x], v.slot_of[e.y]);
+    }
+}
+
+static inline int blocks(long long n, int t) { return (int)((n + t - 1) / t); }
+
+void launch_derive_inputs(const DevView &v, cudaStream_t st) {
+    k_derive<<<blocks(v.N, 256), 256, 0, st>>>(v, 0);
+}
+
+void launch_remap_terms(const DevView &v, cudaStream_t st) {
+    long long n = (long long)v.nb + v.na + v.nt + v.nex;
+    if (n > 0) k_remap<<<blocks(n, 256), 256, 0, st>>>(v);
+}
+
+void launch_nlist_rebuild(const DevView &v, cudaStream_t st) {
+    k_zero_cells<<<blocks(v.total_cells, 256), 256, 0, st>>>(v);
+    k_assign<<<blocks(v.N, 256), 256, 0, st>>>(v);
+    k_scan<<<1, 1024, 0, st>>>(v.flags, v.cell_count, v.cell_start, v.total_cells);
+    k_scatter<<<blocks(v.N, 256), 256, 0, st>>>(v);
+    k_cellsort<<<blocks(v.total_cells, 128), 128, 0, st>>>(v);
+    k_permute_gather<<<blocks(v.N, 256), 256, 0, st>>>(v);
+    k_permute_scatter<<<blocks(v.N, 256), 256, 0, st>>>(v);
+    k_derive<<<blocks(v.N, 256), 256, 0, st>>>(v, 1);
+    long long nt = (long long)v.nb + v.na + v.nt + v.nex;
+    if (nt > 0) k_remap<<<blocks(nt, 256), 256, 0, st>>>(v);
+    k_build<<<blocks((long long)v.N * 32, 256), 256, 0, st>>>(v);
+}
+
+}  // namespace nxm

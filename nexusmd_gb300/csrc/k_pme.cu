@@ -1,0 +1,170 @@
+// PME charge spreading and force gathering (B-spline order 5), one thread per
+// atom over all systems of the batch.
+//
+// Grid index and fraction follow InitparticleIndexAndFraction
+// (core/baseline/src/Forces/NonbondedForce.cpp:51-71) in FP64: t = x / L,
+// t = (t - floor t) K, index = int(t) mod K, fraction = t - int(t) -- the
+// grid is anchored at the origin, not at the box's lower bound.  Spline
+// weights and derivatives follow computeBSplineParameters (:144-182); the
+// spread is :220-260 and the gather :407-461.  In mixed mode the weights are
+// FP32 and the grid is summed as int64 fixed point (bit-reproducible).
+#include "nxm_fft.h"
+#include "nxm_view.h"
+
+namespace nxm {
+
+void launch_fft_convolve(const DevView &v, const FftPlan &p, int energy, cudaStream_t st);
+
+template <typename R>
+__device__ __forceinline__ void bspline5(R dr, R *th, R *dth) {
+    th[4] = 0;
+    th[1] = dr;
+    th[0] = 1 - dr;
+#pragma unroll
+    for (int k = 3; k < 5; k++) {
+        R div = (R)1 / (R)(k - 1);
+        th[k - 1] = div * dr * th[k - 2];
+#pragma unroll
+        for (int l = 1; l < (k - 1); l++)
+            th[k - l - 1] = div * ((dr + l) * th[k - l - 2] + ((R)(k - l) - dr) * th[k - l - 1]);
+        th[0] = div * (1 - dr) * th[0];
+    }
+    dth[0] = -th[0];
+#pragma unroll
+    for (int k = 1; k < 5; k++) dth[k] = th[k - 1] - th[k];
+    R div = (R)0.25;
+    th[4] = div * dr * th[3];
+#pragma unroll
+    for (int l = 1; l < 4; l++) th[4 - l] = div * ((dr + l) * th[3 - l] + ((R)(5 - l) - dr) * th[4 - l]);
+    th[0] = div * (1 - dr) * th[0];
+}
+
+__device__ __forceinline__ void grid_add(long long *g, float v) {
+    atomicAdd(reinterpret_cast<unsigned long long *>(g),
+              static_cast<unsigned long long>(__float2ll_rn(v * 4294967296.0f)));
+}
+__device__ __forceinline__ void grid_add(double *g, double v) { atomicAdd(g, v); }
+
+template <typename R, typename Acc>
+__global__ void __launch_bounds__(128) k_spread(DevView v, const FftSysDev *fs) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= v.N) return;
+    int sys = v.sys_of[s];
+    const SysDev &S = v.sys[sys];
+    if (!S.nb_on) return;
+    const FftSysDev &F = fs[sys];
+    double p[3] = {v.x[s], v.y[s], v.z[s]};
+    int idx[3];
+    R fr[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        double t = p[d] * S.invL[d];
+        t = (t - floor(t)) * F.K[d];
+        int ti = (int)t;
+        fr[d] = (R)(t - ti);
+        idx[d] = ti % F.K[d];
+    }
+    v.pme_idx[s] = make_int4(idx[0], idx[1], idx[2], 0);
+    if (sizeof(R) == 4) {
+        static_cast<float4 *>(v.pme_frac)[s] = make_float4((float)fr[0], (float)fr[1], (float)fr[2], 0.f);
+    } else {
+        double2 *f = static_cast<double2 *>(v.pme_frac);
+        f[2 * s] = make_double2((double)fr[0], (double)fr[1]);
+        f[2 * s + 1] = make_double2((double)fr[2], 0.0);
+    }
+    R th[3][5], dth[3][5];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) bspline5<R>(fr[d], th[d], dth[d]);
+    R q = (R)v.q[s];
+    Acc *g = static_cast<Acc *>(v.grid_acc) + F.roff;
+    int K1 = F.K[1], K2 = F.K[2];
+    for (int ix = 0; ix < 5; ++ix) {
+        int xi = idx[0] + ix;
+        xi -= xi >= F.K[0] ? F.K[0] : 0;
+        R qx = q * th[0][ix];
+        for (int iy = 0; iy < 5; ++iy) {
+            int yi = idx[1] + iy;
+            yi -= yi >= K1 ? K1 : 0;
+            R qxy = qx * th[1][iy];
+            long long row = ((long long)xi * K1 + yi) * K2;
+#pragma unroll
+            for (int iz = 0; iz < 5; ++iz) {
+                int zi = idx[2] + iz;
+                zi -= zi >= K2 ? K2 : 0;
+                grid_add(g + row + zi, qxy * th[2][iz]);
+            }
+        }
+    }
+}
+
+template <typename R, typename Acc>
+__global__ void __launch_bounds__(128) k_gather(DevView v, const FftSysDev *fs) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= v.N) return;
+    int sys = v.sys_of[s];
+    const SysDev &S = v.sys[sys];
+    if (!S.nb_on) return;
+    const FftSysDev &F = fs[sys];
+    int4 id = v.pme_idx[s];
+    R fr[3];
+    if (sizeof(R) == 4) {
+        float4 f = static_cast<const float4 *>(v.pme_frac)[s];
+        fr[0] = (R)f.x;
+        fr[1] = (R)f.y;
+        fr[2] = (R)f.z;
+    } else {
+        const double2 *f = static_cast<const double2 *>(v.pme_frac);
+        double2 a = f[2 * s], b = f[2 * s + 1];
+        fr[0] = (R)a.x;
+        fr[1] = (R)a.y;
+        fr[2] = (R)b.x;
+    }
+    R th[3][5], dth[3][5];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) bspline5<R>(fr[d], th[d], dth[d]);
+    const R *g = static_cast<const R *>(v.grid_real) + F.roff;
+    int K1 = F.K[1], K2 = F.K[2];
+    R fx = 0, fy = 0, fz = 0;
+    for (int ix = 0; ix < 5; ++ix) {
+        int xi = id.x + ix;
+        xi -= xi >= F.K[0] ? F.K[0] : 0;
+        for (int iy = 0; iy < 5; ++iy) {
+            int yi = id.y + iy;
+            yi -= yi >= K1 ? K1 : 0;
+            const R *row = g + ((long long)xi * K1 + yi) * K2;
+            R txy = th[0][ix] * th[1][iy];
+            R dxy = dth[0][ix] * th[1][iy];
+            R tdy = th[0][ix] * dth[1][iy];
+#pragma unroll
+            for (int iz = 0; iz < 5; ++iz) {
+                int zi = id.z + iz;
+                zi -= zi >= K2 ? K2 : 0;
+                R gv = row[zi];
+                fx += dxy * th[2][iz] * gv;
+                fy += tdy * th[2][iz] * gv;
+                fz += txy * dth[2][iz] * gv;
+            }
+        }
+    }
+    R q = (R)v.q[s];
+    using Acc_ = Acc;
+    acc_add(static_cast<Acc_ *>(v.fx) + s, -(q * (fx * (R)(F.K[0] * S.invL[0]))));
+    acc_add(static_cast<Acc_ *>(v.fy) + s, -(q * (fy * (R)(F.K[1] * S.invL[1]))));
+    acc_add(static_cast<Acc_ *>(v.fz) + s, -(q * (fz * (R)(F.K[2] * S.invL[2]))));
+}
+
+void launch_pme(const DevView &v, const FftPlan &plan, int energy, cudaStream_t st) {
+    if (v.N == 0 || plan.nz == 0) return;
+    int nb = (v.N + 127) / 128;
+    if (v.mixed) {
+        k_spread<float, long long><<<nb, 128, 0, st>>>(v, plan.dsys);
+        launch_fft_convolve(v, plan, energy, st);
+        k_gather<float, long long><<<nb, 128, 0, st>>>(v, plan.dsys);
+    } else {
+        k_spread<double, double><<<nb, 128, 0, st>>>(v, plan.dsys);
+        launch_fft_convolve(v, plan, energy, st);
+        k_gather<double, double><<<nb, 128, 0, st>>>(v, plan.dsys);
+    }
+}
+
+}  // namespace nxm

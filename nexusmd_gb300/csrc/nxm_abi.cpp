@@ -1,0 +1,215 @@
+// extern "C" entry points of libnxm_cuda.so for the engine (include/nxm.h).
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/nxm.h"
+#include "nxm_engine.h"
+
+struct nxm_ctx {
+    nxm::Engine eng;
+};
+
+namespace nxm {
+thread_local std::string g_last_error;
+int fail(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+}  // namespace nxm
+
+using nxm::fail;
+
+extern "C" {
+
+const char *nxm_version(void) { return "nexusmd-gb300 0.1 (sm_103a)"; }
+
+const char *nxm_last_error(void) { return nxm::g_last_error.c_str(); }
+
+void nxm_default_options(nxm_options *opt) {
+    if (!opt) return;
+    std::memset(opt, 0, sizeof(*opt));
+    opt->precision = NXM_PRECISION_MIXED;
+    opt->skin = 0.1;
+    opt->rebuild_interval = 10;
+    opt->device = 0;
+    opt->max_neighbors = 0;
+}
+
+static int code_for(const std::string &e) {
+    if (e.find("capacity") != std::string::npos) return NXM_ERR_CAPACITY;
+    if (e.find("non-finite") != std::string::npos) return NXM_ERR_NUMERIC;
+    if (e.find("device") != std::string::npos || e.find("CUDA") != std::string::npos) return NXM_ERR_CUDA;
+    return NXM_ERR_INVALID;
+}
+
+int nxm_create(const nxm_system_desc *systems, int32_t n_systems, const nxm_options *opt,
+               const double *positions, nxm_ctx **out) {
+    if (!systems || n_systems <= 0 || !positions || !out) return fail(NXM_ERR_INVALID, "nxm_create: null argument");
+    *out = nullptr;
+    nxm_options o;
+    nxm_default_options(&o);
+    if (opt) o = *opt;
+    std::vector<nxm::HostSystem> hs(n_systems);
+    for (int s = 0; s < n_systems; ++s) {
+        const nxm_system_desc &d = systems[s];
+        nxm::HostSystem &h = hs[s];
+        if (d.n_atoms <= 0 || !d.masses || !d.charges || !d.sigmas || !d.epsilons)
+            return fail(NXM_ERR_INVALID, "nxm_create: system needs atoms, masses and nonbonded parameters");
+        if ((d.n_bonds > 0 && (!d.bond_atoms || !d.bond_params)) ||
+            (d.n_angles > 0 && (!d.angle_atoms || !d.angle_params)) ||
+            (d.n_torsions > 0 && (!d.torsion_atoms || !d.torsion_params || !d.torsion_periodicity)))
+            return fail(NXM_ERR_INVALID, "nxm_create: term count without arrays");
+        int n = d.n_atoms;
+        h.n = n;
+        h.mass.assign(d.masses, d.masses + n);
+        h.q.assign(d.charges, d.charges + n);
+        h.sig.assign(d.sigmas, d.sigmas + n);
+        h.eps.assign(d.epsilons, d.epsilons + n);
+        if (d.n_bonds > 0) {
+            h.bonds.assign(d.bond_atoms, d.bond_atoms + 2 * (size_t)d.n_bonds);
+            h.bprm.assign(d.bond_params, d.bond_params + 2 * (size_t)d.n_bonds);
+        }
+        if (d.n_angles > 0) {
+            h.angles.assign(d.angle_atoms, d.angle_atoms + 3 * (size_t)d.n_angles);
+            h.aprm.assign(d.angle_params, d.angle_params + 2 * (size_t)d.n_angles);
+        }
+        if (d.n_torsions > 0) {
+            h.torsions.assign(d.torsion_atoms, d.torsion_atoms + 4 * (size_t)d.n_torsions);
+            h.tprm.assign(d.torsion_params, d.torsion_params + 2 * (size_t)d.n_torsions);
+            h.tper.assign(d.torsion_periodicity, d.torsion_periodicity + d.n_torsions);
+        }
+        h.cutoff = d.cutoff;
+        h.tol = d.ewald_tolerance;
+        h.use_switch = d.use_switching;
+        h.sw_dist = d.switching_distance;
+        for (int k = 0; k < 3; ++k) {
+            h.grid[k] = d.grid[k];
+            h.lb[k] = d.box_lb[k];
+            h.ub[k] = d.box_ub[k];
+        }
+        h.box_from_positions = d.box_from_positions;
+        h.force_mask = d.force_mask;
+        h.excl_depth = d.exclusion_depth;
+    }
+    nxm_ctx *c = new (std::nothrow) nxm_ctx;
+    if (!c) return fail(NXM_ERR_INVALID, "out of host memory");
+    std::string e = c->eng.init(hs, o, positions);
+    if (!e.empty()) {
+        delete c;
+        return fail(code_for(e), "nxm_create: " + e);
+    }
+    *out = c;
+    return NXM_OK;
+}
+
+void nxm_destroy(nxm_ctx *ctx) { delete ctx; }
+
+int nxm_n_atoms(const nxm_ctx *ctx, int32_t *n) {
+    if (!ctx || !n) return fail(NXM_ERR_INVALID, "null argument");
+    *n = ctx->eng.n_total();
+    return NXM_OK;
+}
+
+#define NXM_CALL(expr)                                          \
+    do {                                                        \
+        std::string e_ = (expr);                                \
+        if (!e_.empty()) return fail(code_for(e_), e_);         \
+        return NXM_OK;                                          \
+    } while (0)
+
+int nxm_set_positions(nxm_ctx *ctx, const double *xyz) {
+    if (!ctx || !xyz) return fail(NXM_ERR_INVALID, "null argument");
+    NXM_CALL(ctx->eng.set_positions(xyz));
+}
+
+int nxm_set_velocities(nxm_ctx *ctx, const double *xyz) {
+    if (!ctx || !xyz) return fail(NXM_ERR_INVALID, "null argument");
+    NXM_CALL(ctx->eng.set_velocities(xyz));
+}
+
+int nxm_compute_forces(nxm_ctx *ctx) {
+    if (!ctx) return fail(NXM_ERR_INVALID, "null argument");
+    NXM_CALL(ctx->eng.compute_forces());
+}
+
+int nxm_step(nxm_ctx *ctx, int32_t nsteps, double dt) {
+    if (!ctx || nsteps < 0) return fail(NXM_ERR_INVALID, "bad argument");
+    if (nsteps == 0) return NXM_OK;
+    NXM_CALL(ctx->eng.step(nsteps, dt));
+}
+
+int nxm_get_positions(nxm_ctx *ctx, double *xyz) {
+    if (!ctx || !xyz) return fail(NXM_ERR_INVALID, "null argument");
+    NXM_CALL(ctx->eng.get_snapshot(xyz, nullptr, nullptr));
+}
+
+int nxm_get_velocities(nxm_ctx *ctx, double *xyz) {
+    if (!ctx || !xyz) return fail(NXM_ERR_INVALID, "null argument");
+    NXM_CALL(ctx->eng.get_snapshot(nullptr, xyz, nullptr));
+}
+
+int nxm_get_forces(nxm_ctx *ctx, double *xyz) {
+    if (!ctx || !xyz) return fail(NXM_ERR_INVALID, "null argument");
+    NXM_CALL(ctx->eng.get_snapshot(nullptr, nullptr, xyz));
+}
+
+int nxm_get_state(nxm_ctx *ctx, double *xyz, double *vel) {
+    if (!ctx) return fail(NXM_ERR_INVALID, "null argument");
+    NXM_CALL(ctx->eng.get_state(xyz, vel));
+}
+
+int nxm_get_energies(nxm_ctx *ctx, int32_t system, nxm_energies *out) {
+    if (!ctx || !out || system < 0 || system >= ctx->eng.n_systems()) return fail(NXM_ERR_INVALID, "bad argument");
+    ctx->eng.energies(system, out);
+    return NXM_OK;
+}
+
+int nxm_get_box(nxm_ctx *ctx, int32_t system, double lb[3], double ub[3]) {
+    if (!ctx || system < 0 || system >= ctx->eng.n_systems()) return fail(NXM_ERR_INVALID, "bad argument");
+    const nxm::SysHost &h = ctx->eng.sys(system);
+    for (int d = 0; d < 3; ++d) {
+        if (lb) lb[d] = h.lb[d];
+        if (ub) ub[d] = h.ub[d];
+    }
+    return NXM_OK;
+}
+
+int nxm_get_grid(nxm_ctx *ctx, int32_t system, int32_t grid[3]) {
+    if (!ctx || !grid || system < 0 || system >= ctx->eng.n_systems()) return fail(NXM_ERR_INVALID, "bad argument");
+    for (int d = 0; d < 3; ++d) grid[d] = ctx->eng.sys(system).K[d];
+    return NXM_OK;
+}
+
+int nxm_get_alpha(nxm_ctx *ctx, int32_t system, double *alpha) {
+    if (!ctx || !alpha || system < 0 || system >= ctx->eng.n_systems()) return fail(NXM_ERR_INVALID, "bad argument");
+    *alpha = ctx->eng.sys(system).alpha;
+    return NXM_OK;
+}
+
+int64_t nxm_get_pairs(nxm_ctx *ctx, int32_t system, int32_t *pairs, int64_t cap) {
+    if (!ctx || system < 0 || system >= ctx->eng.n_systems() || cap < 0 || (cap > 0 && !pairs))
+        return fail(NXM_ERR_INVALID, "bad argument");
+    std::vector<int> p;
+    std::string e = ctx->eng.pairs(system, p);
+    if (!e.empty()) return fail(code_for(e), e);
+    int64_t n = (int64_t)p.size() / 2;
+    int64_t w = n < cap ? n : cap;
+    if (w > 0) std::memcpy(pairs, p.data(), sizeof(int32_t) * 2 * (size_t)w);
+    return n;
+}
+
+int nxm_time_steps(nxm_ctx *ctx, int32_t nsteps, double dt, double *ms) {
+    if (!ctx || !ms || nsteps <= 0) return fail(NXM_ERR_INVALID, "bad argument");
+    NXM_CALL(ctx->eng.time_steps(nsteps, dt, ms));
+}
+
+int nxm_launches_per_step(nxm_ctx *ctx, int32_t *launches, int32_t *rebuild_launches) {
+    if (!ctx) return fail(NXM_ERR_INVALID, "null argument");
+    if (launches) *launches = ctx->eng.launches_per_step();
+    if (rebuild_launches) *rebuild_launches = ctx->eng.launches_per_rebuild();
+    return NXM_OK;
+}
+
+}  // extern "C"

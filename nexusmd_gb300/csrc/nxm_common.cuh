@@ -1,0 +1,182 @@
+// Device-side definitions shared by every kernel of the NexusMD GB300 engine.
+//
+// Units follow the reference (nm, ps, kJ/mol, e).  Atoms of all systems of a
+// batch live in one flattened "slot" space: system s owns slots
+// [atom_off, atom_off + natoms) and, between neighbour-list rebuilds, slot
+// order is the spatial (cell) order of that system.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace nxm {
+
+// Physical constants exactly as the reference spells them
+// (core/baseline/headers/Forces/NonbondedForce.h:10-27).
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kSqrtPi = 1.77245385090551602729;
+constexpr double kTwoOverSqrtPi = 1.1283791670955126;
+constexpr double kOne4PiEps0 = 138.93545764446428693393;
+
+// Fixed-point scales.  Forces and the mixed-precision charge grid are summed
+// as int64 multiples of 2^-32 (order-independent, so bit-reproducible);
+// energies as multiples of 2^-28 kJ/mol (|E| < 3.4e10).
+constexpr double kForceScale = 4294967296.0;
+constexpr double kForceUnscale = 1.0 / 4294967296.0;
+constexpr double kGridScale = 4294967296.0;
+constexpr double kGridUnscale = 1.0 / 4294967296.0;
+constexpr double kEnergyScale = 268435456.0;
+constexpr double kEnergyUnscale = 1.0 / 268435456.0;
+
+constexpr int kOrder = 5;       // PME B-spline order (NonbondedForce.cpp:474)
+constexpr int kCodeBits = 7;    // list entry = slot (25 bits) | cell-image code (7 bits)
+constexpr uint32_t kSlotMask = (1u << 25) - 1u;
+constexpr int kMaxExclFast = 32;
+
+// Energy slots per system.
+enum EnergyTerm {
+    E_BOND = 0,
+    E_ANGLE,
+    E_TORSION,
+    E_RECIP,
+    E_SELF,
+    E_COUL,
+    E_VDW,
+    E_EXCL,
+    E_KIN,
+    E_SLOTS = 16
+};
+
+// Device error bits (read by the host after each call).
+enum ErrorBits {
+    ERR_NLIST_OVERFLOW = 1,
+    ERR_EXCL_OVERFLOW = 2,
+    ERR_FORCE_RANGE = 4,
+    ERR_NONFINITE = 8,
+    ERR_SKIN_VIOLATION = 16,
+    ERR_CELL = 32,
+};
+
+struct SysDev {
+    double lb[3], ub[3], L[3], invL[3], halfL[3];
+    double cutoff, cut2, alpha, rlist2, sw_dist;
+    float Lf[3], halfLf[3], cut2f, cut2f_lo, cut2f_hi, alphaf, rlist2f, sw_distf, cutofff;
+    int use_switch;
+    int nb_on;                // nonbonded force enabled for this system
+    int atom_off, natoms;
+    int K[3], Kh;             // PME grid, Kh = K[2]/2 + 1
+    long long grid_off;       // first element of this system's real grid
+    long long cgrid_off;      // first element of this system's half complex grid
+    int nc[3], cell_off;      // neighbour cells
+    double cs[3];             // cell edge
+    int tw_off[3];            // twiddle-table offsets for the three FFT lengths
+    float pad_;
+};
+
+// Flags word layout in device memory.
+struct Flags {
+    int error;
+    int rebuild;     // 1 = rebuild the neighbour list this step
+    int since;       // steps since the last rebuild
+    int interval;    // longest allowed gap between rebuilds
+    int skin_hit;    // an atom moved more than skin/2 since the last rebuild
+    int nrebuild;    // rebuilds so far
+    int pad[2];
+};
+
+// ----------------------------------------------------------------- helpers
+
+__device__ __forceinline__ void atomic_add_fixed(long long *a, double v, double scale) {
+    atomicAdd(reinterpret_cast<unsigned long long *>(a),
+              static_cast<unsigned long long>(__double2ll_rn(v * scale)));
+}
+
+__device__ __forceinline__ void acc_add(long long *a, float v) {
+    atomicAdd(reinterpret_cast<unsigned long long *>(a),
+              static_cast<unsigned long long>(__double2ll_rn((double)v * kForceScale)));
+}
+__device__ __forceinline__ void acc_add(double *a, double v) { atomicAdd(a, v); }
+
+__device__ __forceinline__ double acc_value(long long a) { return (double)a * kForceUnscale; }
+__device__ __forceinline__ double acc_value(double a) { return a; }
+
+// The reference's minimum image: one +-L shift when |d| > L/2
+// (core/common/src/PeriodicBoundaryCondition.cpp:93-104).
+__device__ __forceinline__ double min_image(double d, double L, double halfL) {
+    if (d > halfL)
+        d -= L;
+    else if (d < -halfL)
+        d += L;
+    return d;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Energy accumulation: a block-wide FP64 sum per (term, system), added once
+// per block as fixed point when every thread of the block is in one system;
+// otherwise each warp (or lane) adds its own share.  Deterministic.
+__device__ __forceinline__ void energy_add(long long *E, int sys, int term, double v) {
+    const unsigned full = 0xffffffffu;
+    int s0 = __shfl_sync(full, sys, 0);
+    if (__all_sync(full, sys == s0)) {
+        v = warp_sum(v);
+        if ((threadIdx.x & 31) == 0 && v != 0.0) atomic_add_fixed(&E[s0 * E_SLOTS + term], v, kEnergyScale);
+    } else if (v != 0.0) {
+        atomic_add_fixed(&E[sys * E_SLOTS + term], v, kEnergyScale);
+    }
+}
+
+// erfc(x) = exp(-x^2) * g(t), t = 1 / (1 + 0.4 x), x in [0, 4]: degree-8
+// least-squares fit of the scaled complementary error function on Chebyshev
+// nodes of t (derivation and error table: fit_erfcx.py next to this file).
+__device__ __forceinline__ float erfcx_fit(float t) {
+    float g = 8.439681433e-02f;
+    g = fmaf(g, t, -4.465322116e-01f);
+    g = fmaf(g, t, 7.988739227e-01f);
+    g = fmaf(g, t, -5.146168534e-01f);
+    g = fmaf(g, t, 5.139073626e-01f);
+    g = fmaf(g, t, 9.088760701e-02f);
+    g = fmaf(g, t, 2.501002933e-01f);
+    g = fmaf(g, t, 2.228474166e-01f);
+    g = fmaf(g, t, 1.356507552e-04f);
+    return g;
+}
+
+__device__ __forceinline__ float fast_rcp(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ float fast_rsqrt(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// (erf(x) - 2x exp(-x^2)/sqrt(pi)) without the cancellation at small x:
+// for x < 0.6 the Maclaurin series of the difference,
+//   (2/sqrt(pi)) * sum_{n>=1} (-1)^(n+1) x^(2n+1) 2n / (n! (2n+1)),
+// otherwise the direct form.
+__device__ __forceinline__ float erf_minus_gauss(float x, float e /* exp(-x^2) */) {
+    if (x < 0.6f) {
+        float x2 = x * x;
+        float s = -1.0f / 42840.0f;                 // n = 8: 16 / (8! * 17)
+        s = fmaf(s, x2, 1.0f / 5400.0f);            // n = 7
+        s = fmaf(s, x2, -1.0f / 780.0f);            // n = 6
+        s = fmaf(s, x2, 1.0f / 132.0f);             // n = 5
+        s = fmaf(s, x2, -1.0f / 27.0f);             // n = 4
+        s = fmaf(s, x2, 1.0f / 7.0f);               // n = 3
+        s = fmaf(s, x2, -0.4f);                     // n = 2
+        s = fmaf(s, x2, 2.0f / 3.0f);               // n = 1
+        return (float)kTwoOverSqrtPi * x * x2 * s;
+    }
+    return erff(x) - (float)kTwoOverSqrtPi * x * e;
+}
+
+}  // namespace nxm

@@ -1,0 +1,784 @@
+// Host orchestration of the CUDA engine.
+//
+// Set-up reproduces the reference's per-run constants once (box from the
+// atom extent, PME grid rule, Ewald alpha, exclusion sets, B-spline moduli,
+// self energy), where the reference recomputes several of them every step
+// (core/baseline/src/Forces/NonbondedForce.cpp:19-183, :293-321, :515-527).
+// The step is the reference's CalculateForces -> Report -> Integrate
+// (core/baseline/src/Engine.cpp:162-188) as a fixed sequence of kernel
+// launches on one stream, everything resident on the device.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <queue>
+#include <string>
+
+#include "nxm_engine.h"
+
+namespace nxm {
+
+// ------------------------------------------------------------ rebuild gate
+
+__global__ void k_decide(DevView v, int force) {
+    Flags *f = v.flags;
+    int rb = force || f->since >= f->interval || f->skin_hit;
+    f->rebuild = rb;
+    f->skin_hit = 0;
+    f->since = rb ? 1 : f->since + 1;
+    if (rb) f->nrebuild += 1;
+}
+
+void launch_decide_rebuild(const DevView &v, int force, cudaStream_t st) { k_decide<<<1, 1, 0, st>>>(v, force); }
+
+// ------------------------------------------------------------ host maths
+
+static bool smooth235(int n) {
+    if (n < 1) return false;
+    for (int p : {2, 3, 5})
+        while (n % p == 0) n /= p;
+    return n == 1;
+}
+
+// PeriodicBoundaryCondition.cpp:11-88 (water branch: extent, then 1% margin)
+static void box_from_positions(int n, const double *pos, double lb[3], double ub[3], double L[3]) {
+    for (int d = 0; d < 3; ++d) lb[d] = ub[d] = pos[d];
+    for (int i = 0; i < n; ++i)
+        for (int d = 0; d < 3; ++d) {
+            lb[d] = std::min(lb[d], pos[3 * i + d]);
+            ub[d] = std::max(ub[d], pos[3 * i + d]);
+        }
+    double size[3];
+    for (int d = 0; d < 3; ++d) size[d] = std::fabs(ub[d] - lb[d]);
+    for (int d = 0; d < 3; ++d) {
+        double m = 0.01 * size[d];
+        lb[d] -= m;
+        ub[d] += m;
+        L[d] = std::fabs(ub[d] - lb[d]);
+    }
+}
+
+// NonbondedForce.cpp:33-48
+static int pow2_dimension(double box) {
+    int minimum = (int)std::ceil(box) * 10;
+    int p = 1;
+    while (p < minimum) p *= 2;
+    return p;
+}
+
+// NonbondedForce.cpp:75-142: |b(k)|^2 by the direct DFT, with the
+// neighbour average for values below 1e-7.
+static void bspline_moduli(int K, std::vector<double> &mod) {
+    const int ORDER = kOrder;
+    double data[ORDER] = {0, 0, 0, 0, 0};
+    data[ORDER - 1] = 0.0;
+    data[1] = 0.0;
+    data[0] = 1.0;
+    for (int i = 3; i < ORDER; i++) {
+        double div = 1.0 / (i - 1);
+        data[i - 1] = 0.0;
+        for (int j = 1; j < (i - 1); j++) data[i - j - 1] = div * (j * data[i - j - 2] + (i - j) * data[i - j - 1]);
+        data[0] = div * data[0];
+    }
+    double div = 1.0 / (ORDER - 1);
+    data[ORDER - 1] = div * data[ORDER - 2];
+    for (int i = 1; i < (ORDER - 1); i++)
+        data[ORDER - i - 1] = div * (i * data[ORDER - i - 2] + (ORDER - i) * data[ORDER - i - 1]);
+    data[0] = div * data[0];
+    std::vector<double> bs(K + ORDER + 1, 0.0);
+    for (int i = 1; i <= ORDER; i++) bs[i] = data[i - 1];
+    mod.assign(K, 0.0);
+    for (int i = 0; i < K; i++) {
+        double sc = 0.0, ss = 0.0;
+        for (int j = 0; j < K; j++) {
+            double arg = (2 * kPi * i * j) / K;
+            sc += bs[j] * std::cos(arg);
+            ss += bs[j] * std::sin(arg);
+        }
+        mod[i] = sc * sc + ss * ss;
+    }
+    for (int i = 0; i < K; i++)
+        if (mod[i] < 1e-7) mod[i] = (mod[(i - 1 + K) % K] + mod[(i + 1) % K]) / 2.0;
+}
+
+// Exclusions.cpp:7-44 with bondCutoff = depth: every atom reachable through
+// 1..depth bonds.
+static std::string exclusions(const HostSystem &s, std::vector<std::vector<int>> &ex) {
+    int n = s.n;
+    std::vector<std::vector<int>> adj(n);
+    for (size_t b = 0; b < s.bonds.size() / 2; ++b) {
+        int i = s.bonds[2 * b], j = s.bonds[2 * b + 1];
+        if (i < 0 || j < 0 || i >= n || j >= n) return "createExclusions: Illegal particle index in list of bonds";
+        adj[i].push_back(j);
+        adj[j].push_back(i);
+    }
+    ex.assign(n, {});
+    if (s.excl_depth < 1) return "";
+    std::vector<int> dist(n, -1), queue;
+    for (int i = 0; i < n; ++i) {
+        queue.clear();
+        queue.push_back(i);
+        dist[i] = 0;
+        for (size_t h = 0; h < queue.size(); ++h) {
+            int u = queue[h];
+            if (dist[u] == s.excl_depth) continue;
+            for (int w : adj[u])
+                if (dist[w] < 0) {
+                    dist[w] = dist[u] + 1;
+                    queue.push_back(w);
+                    ex[i].push_back(w);
+                }
+        }
+        for (int u : queue) dist[u] = -1;
+        std::sort(ex[i].begin(), ex[i].end());
+    }
+    return "";
+}
+
+// ------------------------------------------------------------ engine
+
+template <typename T>
+T *Engine::dalloc(size_t n) {
+    void *p = nullptr;
+    if (n == 0) n = 1;
+    if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) return nullptr;
+    cudaMemset(p, 0, n * sizeof(T));
+    allocs_.push_back(p);
+    return static_cast<T *>(p);
+}
+
+Engine::~Engine() {
+    if (st_) cudaStreamSynchronize(st_);
+    for (void *p : allocs_) cudaFree(p);
+    fft_plan_free(plan_);
+    if (h_E_) cudaFreeHost(h_E_);
+    if (h_flags_) cudaFreeHost(h_flags_);
+    if (st_) cudaStreamDestroy(st_);
+}
+
+std::string Engine::check(const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return std::string(what) + ": " + cudaGetErrorString(e);
+    return "";
+}
+
+std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_options &opt,
+                         const double *positions) {
+    if (systems.empty()) return "no systems";
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return "no CUDA device";
+    if (opt.device < 0 || opt.device >= ndev) return "bad device ordinal";
+    cudaSetDevice(opt.device);
+    mixed_ = opt.precision == NXM_PRECISION_MIXED ? 1 : 0;
+    interval_ = opt.rebuild_interval > 0 ? opt.rebuild_interval : 1;
+    int S = (int)systems.size();
+    N_ = 0;
+    for (auto &s : systems) {
+        if (s.n <= 0) return "a system has no atoms";
+        N_ += s.n;
+    }
+    if (N_ > (int)kSlotMask) return "too many atoms for the list entry format";
+
+    // ---- per-system constants
+    sysd_.assign(S, SysDev{});
+    sysh_.assign(S, SysHost{});
+    plan_.S = S;
+    plan_.hsys.assign(S, FftSysDev{});
+    std::vector<std::vector<int>> excl_all(N_);
+    std::vector<int2> ex_pairs;
+    int off = 0, cell_off = 0;
+    long long roff = 0, coff = 0;
+    int tw_total = 0;
+    double skin = opt.skin > 0 ? opt.skin : 0.0;
+    int stride = 0;
+    for (int s = 0; s < S; ++s) {
+        const HostSystem &h = systems[s];
+        SysDev &D = sysd_[s];
+        SysHost &H = sysh_[s];
+        const double *p = positions + 3 * (size_t)off;
+        if (h.box_from_positions) {
+            box_from_positions(h.n, p, H.lb, H.ub, H.L);
+        } else {
+            for (int d = 0; d < 3; ++d) {
+                H.lb[d] = h.lb[d];
+                H.ub[d] = h.ub[d];
+                H.L[d] = std::fabs(h.ub[d] - h.lb[d]);
+            }
+        }
+        if (!(h.cutoff > 0)) return "cutoff must be positive";
+        for (int d = 0; d < 3; ++d)
+            if (!(H.L[d] >= 2 * h.cutoff)) return "box edge shorter than twice the cutoff";
+        if (!(h.tol > 0 && h.tol < 0.5)) return "ewald tolerance must be in (0, 0.5)";
+        for (int d = 0; d < 3; ++d) {
+            H.K[d] = h.grid[0] > 0 ? h.grid[d] : pow2_dimension(H.L[d]);
+            if (!smooth235(H.K[d]) || H.K[d] < 5) return "PME grid sizes must be 2^a 3^b 5^c and >= 5";
+            if (H.K[d] > 1024) return "PME grid size above 1024";
+        }
+        H.alpha = (1.0 / h.cutoff) * std::sqrt(-std::log(2.0 * h.tol));
+        double sk = skin;
+        for (int d = 0; d < 3; ++d) sk = std::min(sk, 0.5 * H.L[d] - h.cutoff);
+        H.rlist = h.cutoff + std::max(sk, 0.0);
+        H.atom_off = off;
+        H.natoms = h.n;
+        H.force_mask = h.force_mask;
+        // self energy (NonbondedForce.cpp:515-527)
+        double self = 0.0;
+        for (int i = 0; i < h.n; ++i) self -= kOne4PiEps0 * h.q[i] * h.q[i] * H.alpha / kSqrtPi;
+        H.self_energy = self;
+
+        for (int d = 0; d < 3; ++d) {
+            D.lb[d] = H.lb[d];
+            D.ub[d] = H.ub[d];
+            D.L[d] = H.L[d];
+            D.invL[d] = 1 / H.L[d];
+            D.halfL[d] = 0.5 * H.L[d];
+            D.Lf[d] = (float)H.L[d];
+            D.halfLf[d] = (float)(0.5 * H.L[d]);
+            D.K[d] = H.K[d];
+            int nc = (int)std::floor(H.L[d] / (0.5 * H.rlist));
+            nc = std::max(1, std::min(nc, 1023));
+            D.nc[d] = nc;
+            D.cs[d] = H.L[d] / nc;
+        }
+        D.cutoff = h.cutoff;
+        D.cut2 = h.cutoff * h.cutoff;
+        D.alpha = H.alpha;
+        D.rlist2 = H.rlist * H.rlist;
+        D.sw_dist = h.sw_dist;
+        D.use_switch = h.use_switch;
+        D.nb_on = (h.force_mask & NXM_FORCE_NONBONDED) ? 1 : 0;
+        D.cut2f = (float)D.cut2;
+        D.cut2f_lo = (float)(D.cut2 * (1.0 - 1e-5));
+        D.cut2f_hi = (float)(D.cut2 * (1.0 + 1e-5));
+        D.alphaf = (float)H.alpha;
+        D.rlist2f = (float)D.rlist2;
+        D.sw_distf = (float)h.sw_dist;
+        D.cutofff = (float)h.cutoff;
+        D.atom_off = off;
+        D.natoms = h.n;
+        D.Kh = H.K[2] / 2 + 1;
+        D.grid_off = roff;
+        D.cgrid_off = coff;
+        D.cell_off = cell_off;
+        cell_off += D.nc[0] * D.nc[1] * D.nc[2];
+
+        FftSysDev &F = plan_.hsys[s];
+        for (int d = 0; d < 3; ++d) F.K[d] = H.K[d];
+        F.Kh = D.Kh;
+        F.roff = roff;
+        F.coff = coff;
+        for (int d = 0; d < 3; ++d) {
+            F.tw[d] = tw_total;
+            D.tw_off[d] = tw_total;
+            tw_total += H.K[d];
+        }
+        roff += (long long)H.K[0] * H.K[1] * H.K[2];
+        coff += (long long)H.K[0] * H.K[1] * D.Kh;
+
+        // exclusions (batch-global original indices)
+        std::vector<std::vector<int>> ex;
+        std::string err = exclusions(h, ex);
+        if (!err.empty()) return err;
+        for (int i = 0; i < h.n; ++i) {
+            for (int j : ex[i]) {
+                excl_all[off + i].push_back(off + j);
+                if (j > i) ex_pairs.push_back(make_int2(off + i, off + j));
+            }
+        }
+        // list capacity from the density
+        double vol = H.L[0] * H.L[1] * H.L[2];
+        double expect = 4.0 / 3.0 * kPi * H.rlist * H.rlist * H.rlist * h.n / vol;
+        int cap = (int)(1.6 * expect + 64);
+        stride = std::max(stride, cap);
+        off += h.n;
+    }
+    if (opt.max_neighbors > 0) stride = opt.max_neighbors;
+    stride = (stride + 31) / 32 * 32;
+
+    // ---- device memory
+    cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking);
+    v_ = DevView{};
+    v_.N = N_;
+    v_.S = S;
+    v_.mixed = mixed_;
+    v_.stride = stride;
+    SysDev *dsys = dalloc<SysDev>(S);
+    cudaMemcpy(dsys, sysd_.data(), sizeof(SysDev) * S, cudaMemcpyHostToDevice);
+    v_.sys = dsys;
+    v_.sys_of = dalloc<int>(N_);
+    v_.orig = dalloc<int>(N_);
+    v_.slot_of = dalloc<int>(N_);
+    double **dbl[] = {&v_.x, &v_.y, &v_.z, &v_.vx, &v_.vy, &v_.vz, &v_.mass, &v_.invm, &v_.q, &v_.sig, &v_.eps};
+    for (double **d : dbl) *d = dalloc<double>(N_);
+    if (mixed_) {
+        v_.pf = dalloc<float4>(N_);
+        v_.ljf = dalloc<float2>(N_);
+        v_.fx = dalloc<long long>(N_);
+        v_.fy = dalloc<long long>(N_);
+        v_.fz = dalloc<long long>(N_);
+    } else {
+        v_.qs = dalloc<double>(N_);
+        v_.ljd = dalloc<double2>(N_);
+        v_.fx = dalloc<double>(N_);
+        v_.fy = dalloc<double>(N_);
+        v_.fz = dalloc<double>(N_);
+    }
+    v_.cell3 = dalloc<int>(N_);
+    v_.total_cells = cell_off;
+    v_.cell_key = dalloc<int>(N_);
+    v_.cell_count = dalloc<int>(cell_off + 1);
+    v_.cell_start = dalloc<int>(cell_off + 1);
+    v_.cell_fill = dalloc<int>(cell_off + 1);
+    v_.new_orig = dalloc<int>(N_);
+    v_.nlist = dalloc<uint32_t>((size_t)N_ * stride);
+    v_.ncount = dalloc<int>(N_);
+    v_.dtab = dalloc<float4>((size_t)S * 128);
+    v_.xref = dalloc<double>(3 * (size_t)N_);
+    v_.tmp = dalloc<double>(11 * (size_t)N_);
+    if (!v_.nlist || !v_.tmp) return "device allocation failed (neighbour list)";
+
+    // host staging in original order (slot = original index until the first sort)
+    std::vector<int> sys_of(N_), iota(N_);
+    std::vector<double> hx(N_), hy(N_), hz(N_), hm(N_), him(N_), hq(N_), hs(N_), he(N_);
+    {
+        int o = 0;
+        for (int s = 0; s < S; ++s) {
+            const HostSystem &h = systems[s];
+            for (int i = 0; i < h.n; ++i, ++o) {
+                sys_of[o] = s;
+                iota[o] = o;
+                hx[o] = positions[3 * (size_t)o];
+                hy[o] = positions[3 * (size_t)o + 1];
+                hz[o] = positions[3 * (size_t)o + 2];
+                hm[o] = h.mass[i];
+                him[o] = (h.mass[i] == 0.0) ? 0.0 : 1.0 / h.mass[i];  // VerletIntegration.cpp:37-45
+                hq[o] = h.q[i];
+                hs[o] = h.sig[i];
+                he[o] = h.eps[i];
+            }
+        }
+    }
+    auto up = [&](void *dst, const void *src, size_t bytes) { cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice); };
+    up(v_.sys_of, sys_of.data(), sizeof(int) * N_);
+    up(v_.orig, iota.data(), sizeof(int) * N_);
+    up(v_.slot_of, iota.data(), sizeof(int) * N_);
+    up(v_.x, hx.data(), sizeof(double) * N_);
+    up(v_.y, hy.data(), sizeof(double) * N_);
+    up(v_.z, hz.data(), sizeof(double) * N_);
+    up(v_.mass, hm.data(), sizeof(double) * N_);
+    up(v_.invm, him.data(), sizeof(double) * N_);
+    up(v_.q, hq.data(), sizeof(double) * N_);
+    up(v_.sig, hs.data(), sizeof(double) * N_);
+    up(v_.eps, he.data(), sizeof(double) * N_);
+
+    // cell-image displacement table: code (ox,oy,oz) -> -(o . cs)
+    std::vector<float4> dt((size_t)S * 128, make_float4(0, 0, 0, 0));
+    for (int s = 0; s < S; ++s)
+        for (int ox = -2; ox <= 2; ++ox)
+            for (int oy = -2; oy <= 2; ++oy)
+                for (int oz = -2; oz <= 2; ++oz) {
+                    int code = (ox + 2) * 25 + (oy + 2) * 5 + (oz + 2);
+                    dt[(size_t)s * 128 + code] = make_float4((float)(-ox * sysd_[s].cs[0]), (float)(-oy * sysd_[s].cs[1]),
+                                                             (float)(-oz * sysd_[s].cs[2]), 0.f);
+                }
+    up(v_.dtab, dt.data(), sizeof(float4) * dt.size());
+
+    // exclusion CSR (batch-global original indices)
+    std::vector<int> eoff(N_ + 1, 0), elst;
+    for (int i = 0; i < N_; ++i) {
+        eoff[i + 1] = eoff[i] + (int)excl_all[i].size();
+        elst.insert(elst.end(), excl_all[i].begin(), excl_all[i].end());
+    }
+    v_.excl_off = dalloc<int>(N_ + 1);
+    v_.excl_lst = dalloc<int>(elst.size());
+    up(v_.excl_off, eoff.data(), sizeof(int) * (N_ + 1));
+    if (!elst.empty()) up(v_.excl_lst, elst.data(), sizeof(int) * elst.size());
+
+    // terms (batch-global original indices); kinds disabled by the force mask get a zero count
+    std::vector<int2> bo;
+    std::vector<double2> bp, ap, tp;
+    std::vector<int4> ao, to;
+    std::vector<int> tper;
+    {
+        int o = 0;
+        for (int s = 0; s < S; ++s) {
+            const HostSystem &h = systems[s];
+            if (h.force_mask & NXM_FORCE_BOND)
+                for (size_t b = 0; b < h.bonds.size() / 2; ++b) {
+                    bo.push_back(make_int2(o + h.bonds[2 * b], o + h.bonds[2 * b + 1]));
+                    bp.push_back(make_double2(h.bprm[2 * b], h.bprm[2 * b + 1]));
+                }
+            if (h.force_mask & NXM_FORCE_ANGLE)
+                for (size_t a = 0; a < h.angles.size() / 3; ++a) {
+                    ao.push_back(make_int4(o + h.angles[3 * a], o + h.angles[3 * a + 1], o + h.angles[3 * a + 2], 0));
+                    ap.push_back(make_double2(h.aprm[2 * a], h.aprm[2 * a + 1]));
+                }
+            if (h.force_mask & NXM_FORCE_TORSION)
+                for (size_t t = 0; t < h.torsions.size() / 4; ++t) {
+                    to.push_back(make_int4(o + h.torsions[4 * t], o + h.torsions[4 * t + 1], o + h.torsions[4 * t + 2],
+                                           o + h.torsions[4 * t + 3]));
+                    tp.push_back(make_double2(h.tprm[2 * t], h.tprm[2 * t + 1]));
+                    tper.push_back(h.tper[t]);
+                }
+            for (size_t k = 0; k < h.angles.size(); ++k)
+                if (h.angles[k] < 0 || h.angles[k] >= h.n) return "angle atom index out of range";
+            for (size_t k = 0; k < h.torsions.size(); ++k)
+                if (h.torsions[k] < 0 || h.torsions[k] >= h.n) return "torsion atom index out of range";
+            o += h.n;
+        }
+    }
+    v_.nb = (int)bo.size();
+    v_.na = (int)ao.size();
+    v_.nt = (int)to.size();
+    v_.bond_orig = dalloc<int2>(v_.nb);
+    v_.bond_slot = dalloc<int2>(v_.nb);
+    v_.bond_prm = dalloc<double2>(v_.nb);
+    v_.angle_orig = dalloc<int4>(v_.na);
+    v_.angle_slot = dalloc<int4>(v_.na);
+    v_.angle_prm = dalloc<double2>(v_.na);
+    v_.tors_orig = dalloc<int4>(v_.nt);
+    v_.tors_slot = dalloc<int4>(v_.nt);
+    v_.tors_prm = dalloc<double2>(v_.nt);
+    v_.tors_per = dalloc<int>(v_.nt);
+    if (v_.nb) {
+        up(v_.bond_orig, bo.data(), sizeof(int2) * v_.nb);
+        up(v_.bond_prm, bp.data(), sizeof(double2) * v_.nb);
+    }
+    if (v_.na) {
+        up(v_.angle_orig, ao.data(), sizeof(int4) * v_.na);
+        up(v_.angle_prm, ap.data(), sizeof(double2) * v_.na);
+    }
+    if (v_.nt) {
+        up(v_.tors_orig, to.data(), sizeof(int4) * v_.nt);
+        up(v_.tors_prm, tp.data(), sizeof(double2) * v_.nt);
+        up(v_.tors_per, tper.data(), sizeof(int) * v_.nt);
+    }
+    // exclusion correction pairs: only for systems with nonbonded enabled
+    {
+        std::vector<int2> keep;
+        for (auto &e : ex_pairs)
+            if (sysh_[sys_of[e.x]].force_mask & NXM_FORCE_NONBONDED) keep.push_back(e);
+        ex_pairs.swap(keep);
+    }
+    v_.nex = (int)ex_pairs.size();
+    v_.ex_orig = dalloc<int2>(v_.nex);
+    v_.ex_slot = dalloc<int2>(v_.nex);
+    if (v_.nex) up(v_.ex_orig, ex_pairs.data(), sizeof(int2) * v_.nex);
+
+    // ---- PME
+    bool any_nb = false;
+    for (auto &h : sysh_) any_nb |= (h.force_mask & NXM_FORCE_NONBONDED) != 0;
+    v_.total_grid = roff;
+    v_.total_cgrid = coff;
+    size_t rsz = mixed_ ? sizeof(float) : sizeof(double);
+    size_t csz = 2 * rsz;
+    if (any_nb) {
+        v_.grid_acc = mixed_ ? (void *)dalloc<long long>(roff) : (void *)dalloc<double>(roff);
+        v_.grid_real = mixed_ ? (void *)dalloc<float>(roff) : (void *)dalloc<double>(roff);
+        v_.grid_cplx = mixed_ ? (void *)dalloc<float2>(coff) : (void *)dalloc<double2>(coff);
+        v_.eterm = mixed_ ? (void *)dalloc<float>(coff) : (void *)dalloc<double>(coff);
+        v_.twiddle = mixed_ ? (void *)dalloc<float2>(tw_total) : (void *)dalloc<double2>(tw_total);
+        if (!v_.grid_acc || !v_.grid_cplx) return "device allocation failed (PME grids)";
+        (void)csz;
+        // twiddles exp(-2 pi i t / K)
+        std::vector<double> tw(2 * (size_t)tw_total);
+        for (int s = 0; s < S; ++s)
+            for (int d = 0; d < 3; ++d) {
+                int K = sysh_[s].K[d];
+                for (int t = 0; t < K; ++t) {
+                    double a = -2.0 * kPi * (double)t / (double)K;
+                    tw[2 * ((size_t)plan_.hsys[s].tw[d] + t)] = std::cos(a);
+                    tw[2 * ((size_t)plan_.hsys[s].tw[d] + t) + 1] = std::sin(a);
+                }
+            }
+        if (mixed_) {
+            std::vector<float> twf(tw.begin(), tw.end());
+            up(v_.twiddle, twf.data(), sizeof(float) * twf.size());
+        } else {
+            up(v_.twiddle, tw.data(), sizeof(double) * tw.size());
+        }
+        // influence function on the half spectrum, NonbondedForce.cpp:323-388
+        std::vector<double> et((size_t)coff, 0.0);
+        for (int s = 0; s < S; ++s) {
+            const SysHost &H = sysh_[s];
+            if (!(H.force_mask & NXM_FORCE_NONBONDED)) continue;
+            std::vector<double> mod[3];
+            for (int d = 0; d < 3; ++d) bspline_moduli(H.K[d], mod[d]);
+            double recip[3] = {1 / H.L[0], 1 / H.L[1], 1 / H.L[2]};
+            double one_4pi_eps = kOne4PiEps0 / 1.0;
+            double factor = kPi * kPi / (H.alpha * H.alpha);
+            double boxfactor = kPi * H.L[0] * H.L[1] * H.L[2];
+            int K0 = H.K[0], K1 = H.K[1], K2 = H.K[2], Kh = K2 / 2 + 1;
+            int maxkx = (K0 + 1) / 2, maxky = (K1 + 1) / 2, maxkz = (K2 + 1) / 2;
+            double *e = et.data() + plan_.hsys[s].coff;
+            for (int kx = 0; kx < K0; ++kx) {
+                double mx = (kx < maxkx) ? kx : (kx - K0);
+                double mhx = mx * recip[0];
+                double bx = boxfactor * mod[0][kx];
+                for (int ky = 0; ky < K1; ++ky) {
+                    double my = (ky < maxky) ? ky : (ky - K1);
+                    double mhy = my * recip[1];
+                    double by = mod[1][ky];
+                    for (int kz = 0; kz < Kh; ++kz) {
+                        size_t idx = ((size_t)kx * K1 + ky) * Kh + kz;
+                        if (kx == 0 && ky == 0 && kz == 0) {
+                            e[idx] = 0.0;
+                            continue;
+                        }
+                        double mz = (kz < maxkz) ? kz : (kz - K2);
+                        double mhz = mz * recip[2];
+                        double m2 = mhx * mhx + mhy * mhy + mhz * mhz;
+                        double bz = mod[2][kz];
+                        double denom = m2 * bx * by * bz;
+                        e[idx] = one_4pi_eps * std::exp(-factor * m2) / denom;
+                    }
+                }
+            }
+        }
+        if (mixed_) {
+            std::vector<float> ef(et.begin(), et.end());
+            up(v_.eterm, ef.data(), sizeof(float) * ef.size());
+        } else {
+            up(v_.eterm, et.data(), sizeof(double) * et.size());
+        }
+        v_.pme_idx = dalloc<int4>(N_);
+        v_.pme_frac = mixed_ ? (void *)dalloc<float4>(N_) : (void *)dalloc<double2>(2 * (size_t)N_);
+        // FFT work lists only for systems with nonbonded forces: systems
+        // without them keep an empty grid that no block touches
+        fft_plan_build(plan_, mixed_);
+    }
+    // systems without nonbonded forces: zero their charges in the PME and
+    // pair paths by skipping them entirely (no list, no grid)
+    v_.E = dalloc<long long>((size_t)S * E_SLOTS);
+    v_.flags = dalloc<Flags>(1);
+    {
+        Flags f{};
+        f.interval = interval_;
+        up(v_.flags, &f, sizeof(f));
+    }
+    v_.snap_x = dalloc<double>(3 * (size_t)N_);
+    v_.snap_v = dalloc<double>(3 * (size_t)N_);
+    v_.snap_f = dalloc<double>(3 * (size_t)N_);
+    v_.skin_half2 = skin > 0 ? 0.25 * skin * skin : 0.0;
+    v_.force_mask = 0;
+    for (auto &h : sysh_) v_.force_mask |= h.force_mask;
+    cudaMallocHost(&h_E_, sizeof(long long) * S * E_SLOTS);
+    cudaMallocHost(&h_flags_, sizeof(Flags));
+    energies_.assign((size_t)S * E_SLOTS, 0.0);
+    for (void *p : allocs_)
+        if (!p) return "device allocation failed";
+    launch_derive_inputs(v_, st_);
+    force_rebuild_ = true;
+    std::string e = check("set-up");
+    if (!e.empty()) return e;
+    cudaStreamSynchronize(st_);
+    return check("set-up");
+}
+
+std::string Engine::set_positions(const double *xyz) {
+    // positions arrive in original order; the slot order is re-derived
+    // from them by the forced rebuild of the next evaluation
+    std::vector<double> h(3 * (size_t)N_);
+    std::vector<int> orig(N_);
+    cudaMemcpy(orig.data(), v_.orig, sizeof(int) * N_, cudaMemcpyDeviceToHost);
+    std::vector<double> hx(N_), hy(N_), hz(N_);
+    for (int s = 0; s < N_; ++s) {
+        int o = orig[s];
+        hx[s] = xyz[3 * (size_t)o];
+        hy[s] = xyz[3 * (size_t)o + 1];
+        hz[s] = xyz[3 * (size_t)o + 2];
+    }
+    cudaMemcpy(v_.x, hx.data(), sizeof(double) * N_, cudaMemcpyHostToDevice);
+    cudaMemcpy(v_.y, hy.data(), sizeof(double) * N_, cudaMemcpyHostToDevice);
+    cudaMemcpy(v_.z, hz.data(), sizeof(double) * N_, cudaMemcpyHostToDevice);
+    launch_derive_inputs(v_, st_);
+    force_rebuild_ = true;
+    cudaStreamSynchronize(st_);
+    return check("set_positions");
+}
+
+std::string Engine::set_velocities(const double *xyz) {
+    std::vector<int> orig(N_);
+    cudaMemcpy(orig.data(), v_.orig, sizeof(int) * N_, cudaMemcpyDeviceToHost);
+    std::vector<double> hx(N_), hy(N_), hz(N_);
+    for (int s = 0; s < N_; ++s) {
+        int o = orig[s];
+        hx[s] = xyz[3 * (size_t)o];
+        hy[s] = xyz[3 * (size_t)o + 1];
+        hz[s] = xyz[3 * (size_t)o + 2];
+    }
+    cudaMemcpy(v_.vx, hx.data(), sizeof(double) * N_, cudaMemcpyHostToDevice);
+    cudaMemcpy(v_.vy, hy.data(), sizeof(double) * N_, cudaMemcpyHostToDevice);
+    cudaMemcpy(v_.vz, hz.data(), sizeof(double) * N_, cudaMemcpyHostToDevice);
+    return check("set_velocities");
+}
+
+// Force kernels of one evaluation (everything but the integrator).
+static int force_launches(const DevView &v, const FftPlan &plan, int energy, cudaStream_t st) {
+    int n = 0;
+    if (v.nb + v.na + v.nt) {
+        launch_bonded(v, energy, st);
+        ++n;
+    }
+    if (v.force_mask & NXM_FORCE_NONBONDED) {
+        launch_pairs(v, energy, st);
+        ++n;
+        if (v.nex) {
+            launch_exclusions(v, energy, st);
+            ++n;
+        }
+        launch_pme(v, plan, energy, st);
+        n += 7;
+    }
+    return n;
+}
+
+std::string Engine::one_step(double dt, int report) {
+    if (report) cudaMemsetAsync(v_.E, 0, sizeof(long long) * v_.S * E_SLOTS, st_);
+    launch_decide_rebuild(v_, force_rebuild_ ? 1 : 0, st_);
+    force_rebuild_ = false;
+    launch_nlist_rebuild(v_, st_);
+    int n = force_launches(v_, plan_, report, st_);
+    launch_integrate(v_, dt, report, st_);
+    launches_per_step_ = n + 2;        // decide + forces + integrate
+    launches_per_rebuild_ = 14;        // the gated rebuild kernels
+    return check("step");
+}
+
+void Engine::fetch_energies() {
+    cudaMemcpyAsync(h_E_, v_.E, sizeof(long long) * v_.S * E_SLOTS, cudaMemcpyDeviceToHost, st_);
+}
+
+std::string Engine::finish_call() {
+    fetch_energies();
+    cudaMemcpyAsync(h_flags_, v_.flags, sizeof(Flags), cudaMemcpyDeviceToHost, st_);
+    cudaError_t e = cudaStreamSynchronize(st_);
+    if (e != cudaSuccess) return std::string("device: ") + cudaGetErrorString(e);
+    for (size_t k = 0; k < energies_.size(); ++k) energies_[k] = (double)h_E_[k] * kEnergyUnscale;
+    int err = h_flags_[0];
+    if (err & ERR_NLIST_OVERFLOW) return "neighbour list capacity exceeded (raise max_neighbors)";
+    if (err & ERR_NONFINITE) return "non-finite force";
+    return "";
+}
+
+std::string Engine::step(int nsteps, double dt) {
+    for (int k = 0; k < nsteps; ++k) {
+        std::string e = one_step(dt, k == nsteps - 1);
+        if (!e.empty()) return e;
+    }
+    return finish_call();
+}
+
+std::string Engine::compute_forces() {
+    cudaMemsetAsync(v_.E, 0, sizeof(long long) * v_.S * E_SLOTS, st_);
+    launch_decide_rebuild(v_, 1, st_);
+    force_rebuild_ = false;
+    launch_nlist_rebuild(v_, st_);
+    force_launches(v_, plan_, 1, st_);
+    launch_export(v_, 1, st_);
+    std::string e = check("compute_forces");
+    if (!e.empty()) return e;
+    return finish_call();
+}
+
+std::string Engine::time_steps(int nsteps, double dt, double *ms) {
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, st_);
+    for (int k = 0; k < nsteps; ++k) {
+        std::string e = one_step(dt, 0);
+        if (!e.empty()) return e;
+    }
+    cudaEventRecord(b, st_);
+    std::string e = finish_call();
+    float t = 0;
+    cudaEventElapsedTime(&t, a, b);
+    *ms = t;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return e;
+}
+
+std::string Engine::get_snapshot(double *x, double *v, double *f) {
+    cudaStreamSynchronize(st_);
+    size_t b = sizeof(double) * 3 * (size_t)N_;
+    if (x) cudaMemcpy(x, v_.snap_x, b, cudaMemcpyDeviceToHost);
+    if (v) cudaMemcpy(v, v_.snap_v, b, cudaMemcpyDeviceToHost);
+    if (f) cudaMemcpy(f, v_.snap_f, b, cudaMemcpyDeviceToHost);
+    return check("snapshot");
+}
+
+std::string Engine::get_state(double *x, double *v) {
+    // export current x and v (not forces) into the snapshot buffers' copies
+    std::vector<int> orig(N_);
+    cudaStreamSynchronize(st_);
+    cudaMemcpy(orig.data(), v_.orig, sizeof(int) * N_, cudaMemcpyDeviceToHost);
+    std::vector<double> a(N_), b(N_), c(N_);
+    double *src[2][3] = {{v_.x, v_.y, v_.z}, {v_.vx, v_.vy, v_.vz}};
+    double *dst[2] = {x, v};
+    for (int k = 0; k < 2; ++k) {
+        if (!dst[k]) continue;
+        cudaMemcpy(a.data(), src[k][0], sizeof(double) * N_, cudaMemcpyDeviceToHost);
+        cudaMemcpy(b.data(), src[k][1], sizeof(double) * N_, cudaMemcpyDeviceToHost);
+        cudaMemcpy(c.data(), src[k][2], sizeof(double) * N_, cudaMemcpyDeviceToHost);
+        for (int s = 0; s < N_; ++s) {
+            int o = orig[s];
+            dst[k][3 * (size_t)o] = a[s];
+            dst[k][3 * (size_t)o + 1] = b[s];
+            dst[k][3 * (size_t)o + 2] = c[s];
+        }
+    }
+    return check("state");
+}
+
+void Engine::energies(int s, nxm_energies *out) const {
+    const double *e = energies_.data() + (size_t)s * E_SLOTS;
+    const SysHost &H = sysh_[s];
+    std::memset(out, 0, sizeof(*out));
+    out->bond = e[E_BOND];
+    out->angle = e[E_ANGLE];
+    out->torsion = e[E_TORSION];
+    out->kinetic = e[E_KIN];
+    double pe = 0.0;
+    if (H.force_mask & NXM_FORCE_BOND) pe += out->bond;
+    if (H.force_mask & NXM_FORCE_ANGLE) pe += out->angle;
+    if (H.force_mask & NXM_FORCE_TORSION) pe += out->torsion;
+    double reported = pe;
+    if (H.force_mask & NXM_FORCE_NONBONDED) {
+        out->recip = e[E_RECIP];
+        out->self = H.self_energy;
+        out->coulomb = e[E_COUL];
+        out->vdw = e[E_VDW];
+        out->exclusion = e[E_EXCL];
+        double nb = out->recip + out->self + out->coulomb + out->vdw - out->exclusion;
+        pe += nb;
+        // NonbondedForce.cpp:387 assigns the reciprocal energy to the running
+        // total, then self, direct and exclusion terms are added to it
+        reported = out->recip;
+        reported += out->self;
+        reported += out->coulomb + out->vdw;
+        reported -= out->exclusion;
+    }
+    out->potential = pe;
+    out->reported_potential = reported;
+}
+
+std::string Engine::pairs(int s, std::vector<int> &out) {
+    cudaStreamSynchronize(st_);
+    long long cap = 400LL * sysh_[s].natoms + 1024;
+    int *d = nullptr;
+    if (cudaMalloc(&d, sizeof(int) * 2 * cap) != cudaSuccess) return "allocation failed";
+    long long n = launch_collect_pairs(v_, s, d, cap, st_);
+    if (n > cap) {
+        cudaFree(d);
+        cap = n;
+        if (cudaMalloc(&d, sizeof(int) * 2 * cap) != cudaSuccess) return "allocation failed";
+        n = launch_collect_pairs(v_, s, d, cap, st_);
+    }
+    out.resize(2 * (size_t)n);
+    if (n) cudaMemcpy(out.data(), d, sizeof(int) * 2 * n, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return check("pairs");
+}
+
+}  // namespace nxm

@@ -1,0 +1,107 @@
+// Host side of the CUDA engine: set-up of a batch of systems, device memory,
+// and the per-step launch sequence.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "../../include/nxm.h"
+#include "nxm_fft.h"
+#include "nxm_view.h"
+
+namespace nxm {
+
+struct HostSystem {
+    int n = 0;
+    std::vector<double> mass, q, sig, eps;
+    std::vector<int> bonds, angles, torsions, tper;  // flattened atom indices
+    std::vector<double> bprm, aprm, tprm;
+    double cutoff = 1.0, tol = 5e-4;
+    int use_switch = 0;
+    double sw_dist = 0.0;
+    int grid[3] = {0, 0, 0};
+    int box_from_positions = 1;
+    double lb[3] = {0, 0, 0}, ub[3] = {0, 0, 0};
+    int force_mask = 15;
+    int excl_depth = 3;
+};
+
+struct SysHost {
+    double lb[3], ub[3], L[3];
+    double alpha, rlist;
+    int K[3];
+    double self_energy;
+    int atom_off, natoms;
+    int force_mask;
+};
+
+class Engine {
+public:
+    Engine() = default;
+    ~Engine();
+    // Returns an empty string on success, else the error.
+    std::string init(const std::vector<HostSystem> &systems, const nxm_options &opt,
+                     const double *positions);
+    std::string set_positions(const double *xyz);
+    std::string set_velocities(const double *xyz);
+    std::string compute_forces();
+    std::string step(int nsteps, double dt);
+    // Steps with a snapshot on the schedule of the reference's Report
+    // (step 0 and every `interval`-th); `on_report(step)` runs after each.
+    template <typename F>
+    std::string run_reporting(int nsteps, double dt, int interval, F on_report);
+    std::string get_snapshot(double *x, double *v, double *f);
+    std::string get_state(double *x, double *v);
+    void energies(int sys, nxm_energies *out) const;
+    std::string pairs(int sys, std::vector<int> &out);
+    std::string time_steps(int nsteps, double dt, double *ms);
+    int n_total() const { return N_; }
+    int n_systems() const { return (int)sysh_.size(); }
+    const SysHost &sys(int s) const { return sysh_[s]; }
+    int launches_per_step() const { return launches_per_step_; }
+    int launches_per_rebuild() const { return launches_per_rebuild_; }
+
+private:
+    std::string one_step(double dt, int report);
+    std::string check(const char *what);
+    std::string finish_call();
+    void fetch_energies();
+
+    DevView v_{};
+    FftPlan plan_;
+    std::vector<SysDev> sysd_;
+    std::vector<SysHost> sysh_;
+    cudaStream_t st_ = nullptr;
+    int N_ = 0;
+    int mixed_ = 1;
+    int interval_ = 1;
+    bool force_rebuild_ = true;
+    int since_rebuild_ = 0;
+    std::vector<void *> allocs_;
+    std::vector<double> energies_;  // [S][E_SLOTS] decoded
+    long long *h_E_ = nullptr;       // pinned
+    int *h_flags_ = nullptr;         // pinned
+    int launches_per_step_ = 0, launches_per_rebuild_ = 0;
+    template <typename T>
+    T *dalloc(size_t n);
+};
+
+void launch_export(const DevView &v, int with_forces, cudaStream_t st);
+void launch_decide_rebuild(const DevView &v, int force, cudaStream_t st);
+
+template <typename F>
+std::string Engine::run_reporting(int nsteps, double dt, int interval, F on_report) {
+    for (int step = 0; step < nsteps; ++step) {
+        int report = (((step + 1) % interval) == 0) || step == 0;
+        std::string e = one_step(dt, report);
+        if (!e.empty()) return e;
+        if (report) {
+            e = finish_call();
+            if (!e.empty()) return e;
+            if (!on_report(step)) return "report callback failed";
+        }
+    }
+    return finish_call();
+}
+
+}  // namespace nxm

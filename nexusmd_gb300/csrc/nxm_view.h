@@ -1,0 +1,84 @@
+// The engine's device state as one POD of device pointers, passed by value
+// to every kernel, plus the kernel launchers each .cu file defines.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "nxm_common.cuh"
+
+namespace nxm {
+
+struct DevView {
+    int N, S;            // atoms (slots) and systems in the batch
+    int mixed;           // 1: FP32 force math + int64 fixed point; 0: FP64 throughout
+    int force_mask;      // 1 bond, 2 angle, 4 torsion, 8 nonbonded
+    const SysDev *sys;
+    int *sys_of;         // slot -> system
+    int *orig;           // slot -> original atom index (batch-global)
+    int *slot_of;        // original index -> slot
+    // state, slot order
+    double *x, *y, *z, *vx, *vy, *vz, *mass, *invm;
+    double *q, *sig, *eps;          // raw per-atom parameters
+    // derived per-slot inputs of the pair kernels
+    float4 *pf;          // mixed: cell-relative offset (x,y,z), q * sqrt(ke)
+    float2 *ljf;         // mixed: sigma/2, 2 sqrt(eps)
+    double *qs;          // fp64: q * sqrt(ke)
+    double2 *ljd;        // fp64: sigma/2, 2 sqrt(eps)
+    int *cell3;          // slot -> packed cell coordinates (x | y<<10 | z<<20)
+    // force accumulators (long long in mixed mode, double in fp64 mode)
+    void *fx, *fy, *fz;
+    // neighbour list
+    int total_cells;
+    int *cell_key, *cell_count, *cell_start, *cell_fill;
+    int *new_orig;
+    uint32_t *nlist;
+    int *ncount;
+    int stride;
+    float4 *dtab;        // [S][128] cell-image displacement per code
+    double *xref;        // [3][N] positions at the last rebuild
+    int *excl_off, *excl_lst;  // CSR by original index, partners as original indices
+    // scratch used by the permutation
+    double *tmp;         // [11][N]
+    // bonded terms (original and slot indices)
+    int nb, na, nt;
+    int2 *bond_orig, *bond_slot;
+    double2 *bond_prm;   // d, k
+    int4 *angle_orig, *angle_slot;
+    double2 *angle_prm;  // a, k
+    int4 *tors_orig, *tors_slot;
+    double2 *tors_prm;   // k, phase
+    int *tors_per;
+    int nex;
+    int2 *ex_orig, *ex_slot;   // excluded pairs (i < j by original index)
+    int *bond_sys, *angle_sys, *tors_sys, *ex_sys;
+    // PME
+    long long total_grid, total_cgrid;
+    void *grid_acc;      // real grid accumulator: long long (mixed) / double
+    void *grid_real;     // real grid after the inverse transform: float / double
+    void *grid_cplx;     // half complex grid: float2 / double2
+    void *eterm;         // influence function on the half grid: float / double
+    void *twiddle;       // float2 / double2 tables, forward sign
+    int4 *pme_idx;       // per slot grid base index (x, y, z)
+    void *pme_frac;      // per slot fraction: float4 / double4-as-2xdouble2
+    // energies, flags, report snapshot (original order, AoS [N][3])
+    long long *E;
+    Flags *flags;
+    double *snap_x, *snap_v, *snap_f;
+    double skin_half2;   // (skin/2)^2; 0 disables the displacement check
+};
+
+// kernel launchers (one per .cu file group)
+void launch_nlist_rebuild(const DevView &v, cudaStream_t st);
+void launch_derive_inputs(const DevView &v, cudaStream_t st);
+void launch_bonded(const DevView &v, int energy, cudaStream_t st);
+void launch_pairs(const DevView &v, int energy, cudaStream_t st);
+void launch_exclusions(const DevView &v, int energy, cudaStream_t st);
+void launch_pme(const DevView &v, const struct FftPlan &plan, int energy, cudaStream_t st);
+void launch_integrate(const DevView &v, double dt, int report, cudaStream_t st);
+void launch_snapshot_forces(const DevView &v, cudaStream_t st);
+void launch_remap_terms(const DevView &v, cudaStream_t st);
+long long launch_collect_pairs(const DevView &v, int sys, int *out_pairs, long long cap,
+                               cudaStream_t st);
+
+}  // namespace nxm
