@@ -1,0 +1,384 @@
+#!/usr/bin/env python3
+"""Throughput of the NexusMD force-and-integrate step on GB300.
+
+Default workload: the ~94,100-atom chain + flexible-water system in a 9.8 nm
+periodic box (4 chains x 250 residues + 28,700 waters, seeded synthetic
+stand-in), PME grid 100^3, order 5, cutoff 1.0 nm, Ewald tolerance 5e-4,
+neighbour list cutoff + 0.1 nm skin rebuilt at most every 10 steps, leapfrog
+dt = 0.5 fs, mixed precision (FP32 forces, int64 fixed-point force sums, FP64
+positions/velocities/energies).  A "step" is one full force evaluation plus
+the integration update.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference]
+
+Prints one JSON line (rank 0).  value = atom-steps/s over all ranks, timed on
+the device with CUDA events on the engine's stream (max over ranks); e2e =
+the same metric through the C ABI from the host: context creation from host
+arrays plus one nxm_step(1) call per step with the energies and a position
+frame copied back each step.  Under torchrun every rank runs an independent
+replica on its own GPU (weak scaling; the path has no exchange step).
+--impl reference times the CPU oracle (the FP64 restatement of the
+reference's algorithm; the reference itself is x86/Windows-built C++ that is
+not present on the GPU host) on all host cores as independent processes.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DT_PS = 0.0005
+WORKLOADS = {
+    # name: (config number, description)
+    "c3": (3, "config3: 94,100-atom chain+water, 9.8 nm box, PME 100^3, rc 1.0 nm, skin 0.1 nm / 10 steps"),
+    "c2": (2, "config2: 23,800-atom chain+water, 6.2 nm box, PME 64^3, rc 1.0 nm, skin 0.1 nm / 10 steps"),
+    "c1": (1, "config1: 2,700-atom chain+water, 3.0 nm box, PME 32^3, rc 1.0 nm, skin 0.1 nm / 10 steps"),
+    "c5": (5, "config5: ~474,000-atom chain+water, 16.8 nm box, PME 180^3, rc 1.2 nm, tol 1e-5"),
+}
+# algorithmic FP32 flops per in-cutoff pair (FMA = 2): displacement 3,
+# minimum image 6, r^2 5, rsqrt 1, r 1, alpha r 1, erfc + exp 16, Coulomb 6,
+# LJ 10, force accumulation 9, energy 2
+PAIR_FLOPS = 60
+# algorithmic bytes per unit of the HBM-bound kernels
+BYTES = {"spread": ("atom", 20), "gather": ("atom", 44), "integrate": ("atom", 152)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def init_pg(ws):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo")
+    return dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allmax(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self):
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = max(mx, float(r[2]))
+                for k, name in enumerate(names):
+                    if r[5 + k].strip().lower().startswith("active"):
+                        reasons.add(name)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def fp32_peak_tflops(device):
+    """FP32 (no TF32) cuBLAS SGEMM throughput, measured here: the FP32-pipe roof."""
+    import torch
+    torch.backends.cuda.matmul.allow_tf32 = False
+    dev = torch.device("cuda", device)
+    n = 8192
+    a = torch.randn(n, n, device=dev)
+    b = torch.randn(n, n, device=dev)
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize(dev)
+    best = 0.0
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        torch.cuda.synchronize(dev)
+        best = max(best, 2.0 * n ** 3 / (s.elapsed_time(e) * 1e-3) / 1e12)
+    del a, b
+    torch.cuda.empty_cache()
+    return best
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def traffic_from_profiles(kernel, workload):
+    """DRAM bytes per launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        f = line.split()
+        if len(f) >= 3 and f[0] == kernel and f[1] == workload:
+            try:
+                return float(f[2])
+            except ValueError:
+                return None
+    return None
+
+
+def make_system(cfg):
+    from nexusmd_gb300 import synthetic as sy
+    return sy.config_system(cfg)
+
+
+def cpu_baseline(s, steps=2):
+    """FP64 oracle (the reference's algorithm restated in C) on one host core."""
+    import numpy as np
+    from oracle.nxo import Oracle, build
+    build(ref=False)
+    o = Oracle()
+    d = o.describe(s, box_mode=1, lb=[0.0, 0.0, 0.0], ub=list(s.box))
+    t0 = time.perf_counter()
+    phases = o.run_timed(d, s.pos, np.zeros_like(s.pos), DT_PS, steps)
+    dt = time.perf_counter() - t0
+    return {"value": s.n * steps / dt, "unit": "atom-steps/s", "cores": 1, "kind": "port",
+            "sample": "%d steps of the %d-atom system, FP64 oracle (C restatement), 1 core, %.1f s; "
+                      "phase s/step: %s" % (steps, s.n, dt, ", ".join(
+                          "%s %.3f" % (k, v / steps) for k, v in phases.items()))}
+
+
+def accuracy_check(s, eng_mixed):
+    """Force rel-RMS of the mixed engine vs the FP64 oracle on identical positions."""
+    import numpy as np
+    from oracle.nxo import Oracle, build
+    build(ref=False)
+    o = Oracle()
+    box = o.box_explicit([0.0, 0.0, 0.0], list(s.box))
+    eoff, el = o.exclusions(s.n, s.bonds)
+    F0, E0 = o.forces(o.describe(s, box_mode=1, lb=[0, 0, 0], ub=list(s.box)), s.pos, box, eoff, el)
+    eng_mixed.set_positions(s.pos)
+    F = eng_mixed.compute_forces()
+    err = float(np.sqrt(((F - F0) ** 2).sum() / (F0 ** 2).sum()))
+    dmax = float(np.sqrt(((F - F0) ** 2).sum(1)).max())
+    E = eng_mixed.energies()
+    pe_rel = abs(E["potential"] - (E0["bond"] + E0["angle"] + E0["torsion"] + E0["recip"] + E0["self"]
+                                   + E0["coulomb"] + E0["vdw"] - E0["exclusion"]))
+    pe_ref = abs(E0["recip"]) + abs(E0["self"]) + abs(E0["coulomb"]) + abs(E0["vdw"])
+    return {"force_rel_rms": err, "max_atom_force_err": dmax, "pe_rel_err": pe_rel / pe_ref}
+
+
+def native(args):
+    import numpy as np
+    from nexusmd_gb300.engine import Engine, load_library
+    ws, rank, local = dist_env()
+    dist = init_pg(ws)
+    cfg, desc = WORKLOADS[args.workload]
+    s = make_system(cfg)
+    load_library()
+    kw = dict(skin=0.1, rebuild_interval=10, box="explicit", device=local)
+    eng = Engine(s, precision=1, **kw)
+    eng.step(args.warmup, DT_PS)
+    barrier(dist)
+    with Clocks(local) as clk:
+        ms = eng.time_steps(args.steps, DT_PS)
+    ms = allmax(dist, ms)
+    launches, _ = eng.launches_per_step()
+    per_step = ms / args.steps
+    value = ws * s.n * args.steps / (ms * 1e-3)
+
+    # end to end through the C ABI from host arrays: create + per-step calls
+    barrier(dist)
+    t0 = time.perf_counter()
+    eng2 = Engine(s, precision=1, **kw)
+    frame = np.zeros((s.n, 3))
+    for _ in range(args.steps):
+        eng2.step(1, DT_PS)
+        eng2._L.nxm_get_positions(eng2._h, frame)
+    e2e_s = allmax(dist, time.perf_counter() - t0)
+    del eng2
+    h2d = s.n * (3 + 4) * 8 + (len(s.bonds) * 24 + len(s.angles) * 28 + len(s.torsions) * 36)
+    d2h = s.n * 24 + 16 * 8 + 32
+
+    out = {"metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32 forces / i64 fixed-point sums / f64 x,v,E",
+           "data": "synthetic (seeded chain + flexible water, shapes of the named config)",
+           "config": {"workload": desc, "atoms": s.n, "box_nm": float(s.box[0]),
+                      "pme_grid": list(s.grid), "cutoff_nm": s.cutoff, "skin_nm": 0.1,
+                      "rebuild_interval": 10, "dt_fs": DT_PS * 1000, "precision": "mixed",
+                      "replicas": ws, "l2": "inputs larger than L2 (neighbour list %.0f MB per step)"
+                                          % (s.n * 560 * 4 / 1e6)},
+           "e2e": {"value": ws * s.n * args.steps / e2e_s, "unit": "atom-steps/s",
+                   "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h},
+           "gpu_launches": launches * args.steps,
+           "clocks": clk.summary()}
+    out["ns_per_day"] = (1.0 / (per_step * 1e-3)) * DT_PS * 1e-3 * 86400.0
+
+    if rank == 0 and ws == 1:
+        # per-phase device times (CUDA events on the engine's stream)
+        ph = eng.profile(max(20, min(200, args.steps)), DT_PS)
+        npairs = len(eng.pairs())
+        peaks, src = measured_peaks()
+        fp32 = fp32_peak_tflops(local)
+        top = max(ph, key=ph.get)
+        pair_tf = PAIR_FLOPS * npairs / (ph["pairs"] * 1e-3) / 1e12
+        hbm = {}
+        for k, (unit, b) in BYTES.items():
+            if ph.get(k, 0) > 0:
+                gbs = b * s.n / (ph[k] * 1e-3) / 1e9
+                hbm[k] = {"achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                          "frac": gbs / peaks["hbm_gbs"], "bytes_per_%s" % unit: b}
+        out["roofline"] = {"kernel": "k_pairs_mixed (real-space erfc-Coulomb + LJ)", "bound": "fp32",
+                           "achieved": pair_tf, "peak": fp32, "unit": "TFLOP/s",
+                           "frac": pair_tf / fp32,
+                           "peak_source": "FP32 SGEMM (TF32 off) measured in this run",
+                           "algorithmic": "%d flops x %d in-cutoff pairs per launch" % (PAIR_FLOPS, npairs),
+                           "traffic": traffic_from_profiles("k_pairs_mixed", args.workload),
+                           "top_phase": top}
+        out["roofline_hbm"] = dict(hbm, peak_source="MEASURED_PEAKS.json hbm_gbs (%s)" % src)
+        out["phase_ms"] = ph
+        # plain FP64 form of the same engine
+        eng64 = Engine(s, precision=0, **kw)
+        eng64.step(2, DT_PS)
+        k64 = 10 if s.n > 50000 else 20
+        ms64 = eng64.time_steps(k64, DT_PS)
+        del eng64
+        v64 = s.n * k64 / (ms64 * 1e-3)
+        out["fp64_plain"] = {"value": v64, "unit": "atom-steps/s", "ms_per_step": ms64 / k64,
+                             "mixed_over_fp64": value / v64}
+        if not args.no_check:
+            out["accuracy_vs_fp64_oracle"] = accuracy_check(s, eng)
+        if not args.no_cpu:
+            out["cpu_baseline"] = cpu_baseline(s, steps=args.cpu_steps)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def _oracle_worker(cfg, steps, q):
+    import numpy as np
+    from oracle.nxo import Oracle
+    s = make_system(cfg)
+    o = Oracle()
+    d = o.describe(s, box_mode=1, lb=[0.0, 0.0, 0.0], ub=list(s.box))
+    t0 = time.perf_counter()
+    o.run_timed(d, s.pos, np.zeros_like(s.pos), DT_PS, steps)
+    q.put((s.n, time.perf_counter() - t0))
+
+
+def reference(args):
+    """The reference's algorithm on the host cores (oracle port, one process per core)."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    from oracle.nxo import build
+    build(ref=False)
+    cfg, desc = WORKLOADS[args.workload]
+    procs = os.cpu_count() or 1
+    # bounded sample: each process runs min(K, 2) full steps of the workload
+    steps = max(1, min(args.steps, args.ref_steps))
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    ps = [ctx.Process(target=_oracle_worker, args=(cfg, steps, q)) for _ in range(procs)]
+    t0 = time.perf_counter()
+    for p in ps:
+        p.start()
+    res = [q.get() for _ in ps]
+    for p in ps:
+        p.join()
+    wall = time.perf_counter() - t0
+    n = res[0][0]
+    slowest = max(r[1] for r in res)
+    value = procs * n * steps / slowest
+    out = {"impl": "reference", "metric": "atom-steps/s", "value": value, "unit": "atom-steps/s",
+           "n_gpus": ws, "steps": steps, "warmup": 0, "ms_per_step": slowest / steps * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (seeded chain + flexible water, shapes of the named config)",
+           "config": {"workload": desc, "atoms": n, "precision": "fp64 (reference algorithm)",
+                      "replicas": procs},
+           "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": procs, "kind": "port",
+                            "sample": "%d independent processes x %d steps of the %d-atom system "
+                                      "(FP64 C restatement of the reference, single-threaded per "
+                                      "process), wall %.1f s" % (procs, steps, n, wall)},
+           "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=50)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--workload", default="c3", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--ref-steps", type=int, default=2)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-check", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        reference(args)
+    else:
+        native(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -141,6 +141,13 @@ int64_t nxm_get_pairs(nxm_ctx *ctx, int32_t system, int32_t *pairs, int64_t cap)
  * context's stream, after the call's launches); milliseconds. */
 int nxm_time_steps(nxm_ctx *ctx, int32_t nsteps, double dt, double *ms);
 
+/* Average device milliseconds per step of each phase over nsteps steps
+ * (CUDA events between phases on the context's stream; no energies):
+ * [0] list rebuild decision + rebuild, [1] bonded, [2] real-space pairs,
+ * [3] exclusion correction, [4] PME spread, [5] FFT + convolution,
+ * [6] PME gather, [7] integrate.  cap >= 8. */
+int nxm_profile_phases(nxm_ctx *ctx, int32_t nsteps, double dt, double *ms, int32_t cap);
+
 /* Kernel launches one step issues (steady state, no list rebuild). */
 int nxm_launches_per_step(nxm_ctx *ctx, int32_t *launches, int32_t *rebuild_launches);
 

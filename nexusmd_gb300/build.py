@@ -49,7 +49,10 @@ def _compile(src: str, extra: list[str], hdr: str) -> str:
         key = hashlib.sha256(f.read() + hdr.encode() + " ".join(extra).encode()).hexdigest()
     if os.path.exists(obj) and os.path.exists(stamp) and open(stamp).read() == key:
         return obj
+    # -ffp-contract=off: host FP64 set-up code (box, moduli, influence
+    # function) must round like the reference's unfused x86 build on Arm too
     cmd = [nvcc()] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                             "-Xcompiler", "-ffp-contract=off",
                              "-I" + CSRC, "-I" + os.path.join(ROOT, "include")] + extra + ["-c", path, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -153,18 +153,27 @@ __global__ void __launch_bounds__(128) k_gather(DevView v, const FftSysDev *fs) 
     acc_add(static_cast<Acc_ *>(v.fz) + s, -(q * (fz * (R)(F.K[2] * S.invL[2]))));
 }
 
+void launch_spread(const DevView &v, const FftPlan &plan, cudaStream_t st) {
+    int nb = (v.N + 127) / 128;
+    if (v.mixed)
+        k_spread<float, long long><<<nb, 128, 0, st>>>(v, plan.dsys);
+    else
+        k_spread<double, double><<<nb, 128, 0, st>>>(v, plan.dsys);
+}
+
+void launch_gather(const DevView &v, const FftPlan &plan, cudaStream_t st) {
+    int nb = (v.N + 127) / 128;
+    if (v.mixed)
+        k_gather<float, long long><<<nb, 128, 0, st>>>(v, plan.dsys);
+    else
+        k_gather<double, double><<<nb, 128, 0, st>>>(v, plan.dsys);
+}
+
 void launch_pme(const DevView &v, const FftPlan &plan, int energy, cudaStream_t st) {
     if (v.N == 0 || plan.nz == 0) return;
-    int nb = (v.N + 127) / 128;
-    if (v.mixed) {
-        k_spread<float, long long><<<nb, 128, 0, st>>>(v, plan.dsys);
-        launch_fft_convolve(v, plan, energy, st);
-        k_gather<float, long long><<<nb, 128, 0, st>>>(v, plan.dsys);
-    } else {
-        k_spread<double, double><<<nb, 128, 0, st>>>(v, plan.dsys);
-        launch_fft_convolve(v, plan, energy, st);
-        k_gather<double, double><<<nb, 128, 0, st>>>(v, plan.dsys);
-    }
+    launch_spread(v, plan, st);
+    launch_fft_convolve(v, plan, energy, st);
+    launch_gather(v, plan, st);
 }
 
 }  // namespace nxm

@@ -205,6 +205,11 @@ int nxm_time_steps(nxm_ctx *ctx, int32_t nsteps, double dt, double *ms) {
     NXM_CALL(ctx->eng.time_steps(nsteps, dt, ms));
 }
 
+int nxm_profile_phases(nxm_ctx *ctx, int32_t nsteps, double dt, double *ms, int32_t cap) {
+    if (!ctx || !ms || nsteps <= 0 || cap < nxm::kProfilePhases) return fail(NXM_ERR_INVALID, "bad argument");
+    NXM_CALL(ctx->eng.profile(nsteps, dt, ms));
+}
+
 int nxm_launches_per_step(nxm_ctx *ctx, int32_t *launches, int32_t *rebuild_launches) {
     if (!ctx) return fail(NXM_ERR_INVALID, "null argument");
     if (launches) *launches = ctx->eng.launches_per_step();

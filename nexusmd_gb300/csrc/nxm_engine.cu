@@ -639,8 +639,8 @@ std::string Engine::one_step(double dt, int report) {
     launch_nlist_rebuild(v_, st_);
     int n = force_launches(v_, plan_, report, st_);
     launch_integrate(v_, dt, report, st_);
-    launches_per_step_ = n + 2;        // decide + forces + integrate
-    launches_per_rebuild_ = 14;        // the gated rebuild kernels
+    launches_per_rebuild_ = 10;        // gated rebuild kernels, launched every step
+    launches_per_step_ = n + 2 + launches_per_rebuild_;  // decide + rebuild + forces + integrate
     return check("step");
 }
 
@@ -697,6 +697,49 @@ std::string Engine::time_steps(int nsteps, double dt, double *ms) {
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     return e;
+}
+
+// Average device time per step of each phase over nsteps steps, from CUDA
+// events recorded on the engine's stream between the phases:
+// 0 list decision + rebuild, 1 bonded, 2 pairs, 3 exclusions, 4 spread,
+// 5 FFT + convolution, 6 gather, 7 integrate.
+std::string Engine::profile(int nsteps, double dt, double *ms) {
+    const int P = kProfilePhases;
+    cudaEvent_t ev[P + 1];
+    for (auto &e : ev) cudaEventCreate(&e);
+    double acc[P] = {0};
+    for (int k = 0; k < nsteps; ++k) {
+        cudaEventRecord(ev[0], st_);
+        launch_decide_rebuild(v_, force_rebuild_ ? 1 : 0, st_);
+        force_rebuild_ = false;
+        launch_nlist_rebuild(v_, st_);
+        cudaEventRecord(ev[1], st_);
+        if (v_.nb + v_.na + v_.nt) launch_bonded(v_, 0, st_);
+        cudaEventRecord(ev[2], st_);
+        bool nb = (v_.force_mask & NXM_FORCE_NONBONDED) != 0;
+        if (nb) launch_pairs(v_, 0, st_);
+        cudaEventRecord(ev[3], st_);
+        if (nb && v_.nex) launch_exclusions(v_, 0, st_);
+        cudaEventRecord(ev[4], st_);
+        if (nb && plan_.nz) launch_spread(v_, plan_, st_);
+        cudaEventRecord(ev[5], st_);
+        if (nb && plan_.nz) launch_fft_convolve(v_, plan_, 0, st_);
+        cudaEventRecord(ev[6], st_);
+        if (nb && plan_.nz) launch_gather(v_, plan_, st_);
+        cudaEventRecord(ev[7], st_);
+        launch_integrate(v_, dt, 0, st_);
+        cudaEventRecord(ev[8], st_);
+        cudaError_t e = cudaEventSynchronize(ev[8]);
+        if (e != cudaSuccess) return std::string("profile: ") + cudaGetErrorString(e);
+        for (int p = 0; p < P; ++p) {
+            float t = 0;
+            cudaEventElapsedTime(&t, ev[p], ev[p + 1]);
+            acc[p] += t;
+        }
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    for (int p = 0; p < P; ++p) ms[p] = acc[p] / nsteps;
+    return finish_call();
 }
 
 std::string Engine::get_snapshot(double *x, double *v, double *f) {

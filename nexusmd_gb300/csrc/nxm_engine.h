@@ -11,6 +11,8 @@
 
 namespace nxm {
 
+constexpr int kProfilePhases = 8;
+
 struct HostSystem {
     int n = 0;
     std::vector<double> mass, q, sig, eps;
@@ -55,6 +57,7 @@ public:
     void energies(int sys, nxm_energies *out) const;
     std::string pairs(int sys, std::vector<int> &out);
     std::string time_steps(int nsteps, double dt, double *ms);
+    std::string profile(int nsteps, double dt, double *ms);
     int n_total() const { return N_; }
     int n_systems() const { return (int)sysh_.size(); }
     const SysHost &sys(int s) const { return sysh_[s]; }

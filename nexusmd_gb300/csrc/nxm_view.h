@@ -75,6 +75,9 @@ void launch_bonded(const DevView &v, int energy, cudaStream_t st);
 void launch_pairs(const DevView &v, int energy, cudaStream_t st);
 void launch_exclusions(const DevView &v, int energy, cudaStream_t st);
 void launch_pme(const DevView &v, const struct FftPlan &plan, int energy, cudaStream_t st);
+void launch_spread(const DevView &v, const struct FftPlan &plan, cudaStream_t st);
+void launch_fft_convolve(const DevView &v, const struct FftPlan &plan, int energy, cudaStream_t st);
+void launch_gather(const DevView &v, const struct FftPlan &plan, cudaStream_t st);
 void launch_integrate(const DevView &v, double dt, int report, cudaStream_t st);
 void launch_snapshot_forces(const DevView &v, cudaStream_t st);
 void launch_remap_terms(const DevView &v, cudaStream_t st);

@@ -84,6 +84,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.nxm_get_pairs.argtypes = [C.c_void_p, C.c_int32, np.ctypeslib.ndpointer(np.int32), C.c_int64]
     L.nxm_get_pairs.restype = C.c_int64
     L.nxm_time_steps.argtypes = [C.c_void_p, C.c_int32, C.c_double, C.POINTER(C.c_double)]
+    L.nxm_profile_phases.argtypes = [C.c_void_p, C.c_int32, C.c_double, dp, C.c_int32]
     L.nxm_launches_per_step.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     L.nxm_n_atoms.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
     _lib = L
@@ -242,6 +243,14 @@ class Engine:
             _check(int(n2), "get_pairs")
         p = out[:2 * n].reshape(-1, 2)
         return p[np.lexsort((p[:, 1], p[:, 0]))]
+
+    PHASES = ("rebuild", "bonded", "pairs", "exclusions", "spread", "fft", "gather", "integrate")
+
+    def profile(self, nsteps, dt):
+        """Average device ms per step of each phase (CUDA events on the engine's stream)."""
+        ms = np.zeros(len(self.PHASES))
+        _check(self._L.nxm_profile_phases(self._h, int(nsteps), float(dt), ms, len(ms)), "profile")
+        return dict(zip(self.PHASES, ms.tolist()))
 
     def launches_per_step(self):
         a, b = C.c_int32(), C.c_int32()

@@ -94,40 +94,42 @@ def _place(a, b, c, bond, angle, torsion):
     return c + d2[0] * bc + d2[1] * m + d2[2] * n
 
 
-class _Hash:
-    """Periodic cell hash of points for radius queries (growth-time checks)."""
+class _Grid:
+    """Periodic cell hash of growing chain beads (supports removing the newest)."""
 
-    def __init__(self, box, cell):
+    def __init__(self, box, cell, cap):
         self.box = np.asarray(box, float)
         self.nc = np.maximum((self.box / cell).astype(int), 1)
         self.cell = self.box / self.nc
         self.cells: dict = {}
-        self.pts: list = []
+        self.P = np.zeros((cap, 3))
+        self.chain = np.zeros(cap, np.int64)
+        self.idx = np.zeros(cap, np.int64)
+        self.keys: list = []
+        self.n = 0
 
     def _key(self, p):
-        c = np.floor(np.mod(p, self.box) / self.cell).astype(int) % self.nc
-        return tuple(c)
+        return tuple(np.floor(np.mod(p, self.box) / self.cell).astype(int) % self.nc)
 
-    def add(self, p, tag):
-        self.pts.append((np.array(p), tag))
-        self.cells.setdefault(self._key(p), []).append(len(self.pts) - 1)
+    def add(self, p, chain, idx):
+        k = self._key(p)
+        self.P[self.n], self.chain[self.n], self.idx[self.n] = p, chain, idx
+        self.cells.setdefault(k, []).append(self.n)
+        self.keys.append(k)
+        self.n += 1
 
-    def near(self, p, r, skip=lambda tag: False):
+    def pop(self):
+        self.n -= 1
+        self.cells[self.keys.pop()].pop()
+
+    def around(self, p, reach=1):
         c = np.array(self._key(p))
-        reach = int(math.ceil(r / self.cell.min()))
+        out = []
         for dx in range(-reach, reach + 1):
             for dy in range(-reach, reach + 1):
                 for dz in range(-reach, reach + 1):
-                    k = tuple((c + (dx, dy, dz)) % self.nc)
-                    for idx in self.cells.get(k, ()):
-                        q, tag = self.pts[idx]
-                        if skip(tag):
-                            continue
-                        d = p - q
-                        d -= self.box * np.round(d / self.box)
-                        if d @ d < r * r:
-                            return True
-        return False
+                    out.extend(self.cells.get(tuple((c + (dx, dy, dz)) % self.nc), ()))
+        return np.asarray(out, np.int64)
 
 
 def _contacts(p, L, mol, is_h, min_dist, h_min_dist):
@@ -148,10 +150,16 @@ def _contacts(p, L, mol, is_h, min_dist, h_min_dist):
 # ---------------------------------------------------------------------------
 # builders
 
-def _grow_chain(rng, n_beads, center, radius, box, hsh, chain_id, min_dist):
-    """Self-avoiding compact walk confined to a sphere; returns (pos, r0, theta0)."""
+def _grow_chain(rng, n_beads, center, radius, box, grid, chain_id, min_dist, tries=48):
+    """Self-avoiding compact walk confined to a sphere; returns (pos, r0, theta0).
+
+    Each bead is placed at its bond length and bond angle from the previous
+    two with a random torsion (away from 0/180 degrees); all ``tries``
+    torsions are tested at once against beads of other molecules and beads
+    four or more bonds back, and on a dead end the walk backs up."""
     r0 = rng.uniform(0.10, 0.153, size=n_beads - 1)
     th0 = np.radians(rng.uniform(104.0, 120.0, size=n_beads - 2))
+    L = np.asarray(box, float)
     pos = np.zeros((n_beads, 3))
     pos[0] = center + rng.normal(0, 0.05, 3)
     v = rng.normal(size=3)
@@ -159,44 +167,47 @@ def _grow_chain(rng, n_beads, center, radius, box, hsh, chain_id, min_dist):
     pos[1] = pos[0] + r0[0] * v
     w = np.cross(v, rng.normal(size=3))
     w /= np.linalg.norm(w)
-    ang = th0[0]
-    pos[2] = pos[1] + r0[1] * (-math.cos(ang) * v + math.sin(ang) * w)
+    pos[2] = pos[1] + r0[1] * (-math.cos(th0[0]) * v + math.sin(th0[0]) * w)
     for k in range(3):
-        hsh.add(pos[k], (chain_id, k))
-    i = 3
-    fails = 0
+        grid.add(pos[k], chain_id, k)
+    i, iters = 3, 0
+    stuck = np.zeros(n_beads, np.int64)
     while i < n_beads:
-        placed = False
-        for _ in range(60):
-            tor = rng.uniform(-math.pi, math.pi)
-            if abs(abs(tor) - math.pi) < 0.3 or abs(tor) < 0.3:
-                continue  # keep away from cis/trans-planar and collinear shapes
-            p = _place(pos[i - 3], pos[i - 2], pos[i - 1], r0[i - 1], th0[i - 2], tor)
-            if np.linalg.norm(p - center) > radius:
-                continue
-            # non-excluded partners: beads i-4 and earlier, and other molecules
-            if hsh.near(p, min_dist, skip=lambda tag: tag[0] == chain_id and tag[1] > i - 4):
-                continue
-            placed = True
-            break
-        if placed:
-            pos[i] = p
-            hsh.add(p, (chain_id, i))
+        iters += 1
+        if iters > 200 * n_beads:
+            raise RuntimeError("chain growth stuck")
+        a, b, c = pos[i - 3], pos[i - 2], pos[i - 1]
+        bc = (c - b) / np.linalg.norm(c - b)
+        nrm = np.cross(b - a, bc)
+        nrm /= np.linalg.norm(nrm)
+        m = np.cross(nrm, bc)
+        tor = rng.uniform(0.3, math.pi - 0.3, size=tries) * rng.choice([-1.0, 1.0], size=tries)
+        bl, an = r0[i - 1], th0[i - 2]
+        cand = (c - bl * math.cos(an) * bc
+                + (bl * math.sin(an) * np.cos(tor))[:, None] * m
+                + (bl * math.sin(an) * np.sin(tor))[:, None] * nrm)
+        ok = np.linalg.norm(cand - center, axis=1) <= radius
+        ids = grid.around(c)
+        if len(ids):
+            keep = ~((grid.chain[ids] == chain_id) & (grid.idx[ids] > i - 4))
+            ids = ids[keep]
+        if len(ids) and ok.any():
+            d = cand[:, None, :] - grid.P[ids][None, :, :]
+            d -= L * np.round(d / L)
+            ok &= ((d * d).sum(-1) >= min_dist * min_dist).all(1)
+        hit = np.nonzero(ok)[0]
+        if len(hit):
+            pos[i] = cand[hit[0]]
+            grid.add(pos[i], chain_id, i)
             i += 1
-            fails = 0
         else:
-            fails += 1
-            back = min(i - 3, 2 + fails)
-            if back <= 0 or fails > 200:
+            # back up further every time the walk dead-ends at this bead
+            stuck[i] += 1
+            back = int(min(i - 3, stuck[i]))
+            if back <= 0:
                 raise RuntimeError("chain growth stuck")
-            # drop the last `back` beads from the hash and retry from there
             for _ in range(back):
-                hsh.pts.pop()
-            hsh.cells = {}
-            pts = hsh.pts
-            hsh.pts = []
-            for q, tag in pts:
-                hsh.add(q, tag)
+                grid.pop()
             i -= back
     return pos, r0, th0
 
@@ -204,14 +215,15 @@ def _grow_chain(rng, n_beads, center, radius, box, hsh, chain_id, min_dist):
 def make_system(n_chains: int, residues: int, n_waters: int, box: float, seed: int,
                 cutoff: float = 1.0, ewald_tol: float = 5e-4, grid=(0, 0, 0),
                 beads_per_residue: int = 8, min_dist: float = 0.2, h_min_dist: float = 0.15,
+                jitter: float = 0.004,
                 chain_charge_scale: float = 1.0) -> System:
     """Build a periodic chain + water system in a cubic box of edge ``box`` nm."""
     rng = np.random.Generator(np.random.PCG64(seed))
     L = np.array([box, box, box], float)
-    hsh = _Hash(L, 0.25)
     n_bead = residues * beads_per_residue
-    # chain globules: about 55 beads/nm^3, centres on a coarse lattice
-    radius = (3.0 * n_bead / (4.0 * math.pi * 55.0)) ** (1.0 / 3.0) if n_chains else 0.0
+    beads = _Grid(L, 0.4, max(1, n_chains * n_bead))
+    # chain globules: about 35 beads/nm^3, centres on a coarse lattice
+    radius = (3.0 * n_bead / (4.0 * math.pi * 35.0)) ** (1.0 / 3.0) if n_chains else 0.0
     m = max(1, int(math.ceil(n_chains ** (1.0 / 3.0))))
     centres = []
     for a in range(m):
@@ -221,7 +233,7 @@ def make_system(n_chains: int, residues: int, n_waters: int, box: float, seed: i
     rng.shuffle(centres)
     chains = []
     for ci in range(n_chains):
-        chains.append(_grow_chain(rng, n_bead, centres[ci], radius, L, hsh, ci, min_dist + 0.02))
+        chains.append(_grow_chain(rng, n_bead, centres[ci], radius, L, beads, ci, min_dist + 0.02))
     chain_pos = np.concatenate([c[0] for c in chains]) if chains else np.zeros((0, 3))
     chain_pos = np.mod(chain_pos, L)
 
@@ -318,6 +330,20 @@ def make_system(n_chains: int, residues: int, n_waters: int, box: float, seed: i
     q[o], q[o + 1], q[o + 2] = WATER_Q_O, WATER_Q_H, WATER_Q_H
     sig[o], sig[o + 1], sig[o + 2] = WATER_SIG_O, WATER_SIG_H, WATER_SIG_H
     eps[o], eps[o + 1], eps[o + 2] = WATER_EPS_O, WATER_EPS_H, WATER_EPS_H
+    if jitter > 0:
+        # thermal-scale displacement so that bonds and angles start away from
+        # their minima; atoms whose move would create a contact keep their place
+        moved = pos + np.clip(rng.normal(0.0, jitter, size=pos.shape), -3 * jitter, 3 * jitter)
+        molid = np.concatenate([np.repeat(-1 - np.arange(n_chains), n_bead),
+                                off + np.repeat(np.arange(n_waters), 3)])
+        isH = np.zeros(n_total, bool)
+        isH[o + 1] = True
+        isH[o + 2] = True
+        bad = _contacts(np.mod(moved, L), L, molid, isH, min_dist, h_min_dist)
+        if len(bad):
+            back = np.unique(bad.reshape(-1))
+            moved[back] = pos[back]
+        pos = np.mod(moved, L)
     last_res = (res_seq[-1] if res_seq else 0)
     for w in range(n_waters):
         bonds.append((o[w], o[w] + 1))
