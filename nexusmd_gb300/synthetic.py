@@ -35,7 +35,9 @@ WATER_THETA = math.radians(104.52)
 WATER_KTHETA = 836.8
 WATER_Q_O, WATER_Q_H = -0.834, 0.417
 WATER_SIG_O, WATER_EPS_O = 0.315061, 0.636386
-WATER_SIG_H, WATER_EPS_H = 0.1, 0.0
+# Water H carries a small LJ core so no charged pair is left without repulsion
+# (with eps = 0 a water H can fall onto a negatively charged chain bead).
+WATER_SIG_H, WATER_EPS_H = 0.1, 0.05
 MASS_O, MASS_H = 15.999, 1.008
 CHAIN_MASSES = np.array([12.011, 14.007, 15.999, 32.06])
 CHAIN_MASS_P = np.array([0.55, 0.2, 0.2, 0.05])
@@ -215,7 +217,7 @@ def _grow_chain(rng, n_beads, center, radius, box, grid, chain_id, min_dist, tri
 def make_system(n_chains: int, residues: int, n_waters: int, box: float, seed: int,
                 cutoff: float = 1.0, ewald_tol: float = 5e-4, grid=(0, 0, 0),
                 beads_per_residue: int = 8, min_dist: float = 0.2, h_min_dist: float = 0.15,
-                jitter: float = 0.004,
+                jitter: float = 0.0015,
                 chain_charge_scale: float = 1.0) -> System:
     """Build a periodic chain + water system in a cubic box of edge ``box`` nm."""
     rng = np.random.Generator(np.random.PCG64(seed))
@@ -305,7 +307,7 @@ def make_system(n_chains: int, residues: int, n_waters: int, box: float, seed: i
         qq = rng.normal(0.0, 0.3, size=n_bead)
         q[idx] = (qq - qq.mean()) * chain_charge_scale
         sig[idx] = rng.uniform(0.1, 0.35, size=n_bead)
-        eps[idx] = rng.uniform(0.0, 0.65, size=n_bead)
+        eps[idx] = rng.uniform(0.05, 0.65, size=n_bead)  # within the 0-0.65 range, no bare charges
         for k in range(n_bead - 1):
             bonds.append((idx[k], idx[k + 1]))
             bprm.append((r0[k], rng.uniform(2.5e5, 4.6e5)))
