@@ -20,7 +20,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(HERE, "libnxm_cuda.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["k_neighbor.cu", "k_bonded.cu", "k_nonbonded.cu", "k_fft.cu", "k_pme.cu",
+CUDA_SOURCES = ["k_neighbor.cu", "k_pairs.cu", "k_bonded.cu", "k_nonbonded.cu", "k_fft.cu", "k_pme.cu",
                 "k_integrate.cu", "nxm_engine.cu", "nxm_abi.cpp"]
 HOST_SOURCES = ["nxm_xml.cpp", "nxm_io.cpp", "nxm_dispatcher.cpp"]
 

@@ -80,6 +80,11 @@ __device__ __forceinline__ void small_dft(C *v, int R, typename Cx<C>::R s) {
     }
 }
 
+// floor(a / d) for 0 <= a < 2^22 and d <= 2^12 from a precomputed 1/d:
+// (a + 1/2)/d is at least 1/(2d) away from an integer, far more than the
+// float rounding of the product.
+__device__ __forceinline__ int quot(int a, float inv_d) { return (int)(((float)a + 0.5f) * inv_d); }
+
 // Transform `nlines` contiguous lines of length n held in a (scratch b);
 // returns the buffer that holds the result.  Stockham pass with radix R after
 // sub-transforms of size Ns: element j + r*n/R, twiddled by
@@ -94,11 +99,13 @@ __device__ C *fft_lines(C *a, C *b, int n, int nlines, const int *rad, int np, c
         int m = n / R;
         int step = n / (Ns * R);
         int tot = nlines * m;
+        const float inv_m = 1.0f / (float)m, inv_ns = 1.0f / (float)Ns;
         for (int bi = threadIdx.x; bi < tot; bi += blockDim.x) {
-            int l = bi / m, j = bi - l * m;
+            int l = quot(bi, inv_m), j = bi - l * m;
             const C *src = a + l * n;
             C *dst = b + l * n;
-            int k = j % Ns;
+            int jq = quot(j, inv_ns);
+            int k = j - jq * Ns;
             C v[5];
 #pragma unroll
             for (int r = 0; r < 5; ++r)
@@ -112,7 +119,7 @@ __device__ C *fft_lines(C *a, C *b, int n, int nlines, const int *rad, int np, c
                 }
             }
             small_dft(v, R, (T)sign);
-            int idx = (j / Ns) * Ns * R + k;
+            int idx = jq * Ns * R + k;
 #pragma unroll
             for (int r = 0; r < 5; ++r)
                 if (r < R) dst[idx + r * Ns] = v[r];
@@ -135,7 +142,10 @@ __device__ __forceinline__ const C *tw_table(const DevView &v, int off) {
 }
 
 // ---- z: real -> half spectrum.  Reads the spread accumulator (fixed point
-// in mixed mode) and clears it for the next step.
+// in mixed mode) and clears it for the next step.  Two real lines go through
+// one complex transform (line 2p as the real part, 2p+1 as the imaginary
+// part) and are separated with X_a[k] = (Z[k] + conj Z[n-k]) / 2,
+// X_b[k] = (Z[k] - conj Z[n-k]) / 2i.
 template <typename C, typename Acc>
 __global__ void k_fft_z_fwd(DevView v, const FftSysDev *fs, const FftWork *work, int L) {
     using T = typename Cx<C>::R;
@@ -147,19 +157,33 @@ __global__ void k_fft_z_fwd(DevView v, const FftSysDev *fs, const FftWork *work,
     int nl_total = F.K[0] * F.K[1];
     int l0 = w.unit * L;
     int nl = min(L, nl_total - l0);
-    C *b = a + L * n;
+    int np2 = (nl + 1) >> 1;  // complex lines
+    C *b = a + (L >> 1) * n;
     Acc *acc = static_cast<Acc *>(v.grid_acc) + F.roff + (long long)l0 * n;
-    for (int e = threadIdx.x; e < nl * n; e += blockDim.x) {
-        Acc g = acc[e];
-        acc[e] = (Acc)0;
-        a[e] = Cx<C>::mk((T)grid_value(g), (T)0);
+    for (int e = threadIdx.x; e < np2 * n; e += blockDim.x) {
+        int p = e / n, z = e - p * n;
+        int la = 2 * p, lb = 2 * p + 1;
+        Acc ga = acc[(long long)la * n + z];
+        acc[(long long)la * n + z] = (Acc)0;
+        T vb = (T)0;
+        if (lb < nl) {
+            Acc gb = acc[(long long)lb * n + z];
+            acc[(long long)lb * n + z] = (Acc)0;
+            vb = (T)grid_value(gb);
+        }
+        a[e] = Cx<C>::mk((T)grid_value(ga), vb);
     }
     __syncthreads();
-    C *res = fft_lines(a, b, n, nl, F.rad[2], F.np[2], tw_table<C>(v, F.tw[2]), -1);
+    C *res = fft_lines(a, b, n, np2, F.rad[2], F.np[2], tw_table<C>(v, F.tw[2]), -1);
     C *out = static_cast<C *>(v.grid_cplx) + F.coff + (long long)l0 * Kh;
-    for (int e = threadIdx.x; e < nl * Kh; e += blockDim.x) {
-        int l = e / Kh, kz = e - l * Kh;
-        out[e] = res[l * n + kz];
+    for (int e = threadIdx.x; e < np2 * Kh; e += blockDim.x) {
+        int p = e / Kh, k = e - p * Kh;
+        C z = res[p * n + k];
+        C zc = res[p * n + (k == 0 ? 0 : n - k)];
+        // A = (z + conj zc)/2, B = (z - conj zc)/(2i)
+        out[(long long)(2 * p) * Kh + k] = Cx<C>::mk((T)0.5 * (z.x + zc.x), (T)0.5 * (z.y - zc.y));
+        if (2 * p + 1 < nl)
+            out[(long long)(2 * p + 1) * Kh + k] = Cx<C>::mk((T)0.5 * (z.y + zc.y), (T)0.5 * (zc.x - z.x));
     }
 }
 
@@ -235,7 +259,9 @@ __global__ void k_fft_x_conv(DevView v, const FftSysDev *fs, const FftWork *work
     if (energy) energy_add(v.E, w.sys, E_RECIP, 0.5 * esum);
 }
 
-// ---- z inverse: half spectrum -> real grid (Hermitian completion).
+// ---- z inverse: half spectrum -> real grid.  Two Hermitian lines A, B are
+// completed and combined as Z = A + iB; the real and imaginary parts of the
+// inverse transform are the two real output lines.
 template <typename C>
 __global__ void k_fft_z_inv(DevView v, const FftSysDev *fs, const FftWork *work, int L) {
     using T = typename Cx<C>::R;
@@ -247,23 +273,30 @@ __global__ void k_fft_z_inv(DevView v, const FftSysDev *fs, const FftWork *work,
     int nl_total = F.K[0] * F.K[1];
     int l0 = w.unit * L;
     int nl = min(L, nl_total - l0);
-    C *b = a + L * n;
+    int np2 = (nl + 1) >> 1;
+    C *b = a + (L >> 1) * n;
     const C *in = static_cast<const C *>(v.grid_cplx) + F.coff + (long long)l0 * Kh;
-    for (int e = threadIdx.x; e < nl * n; e += blockDim.x) {
-        int l = e / n, k = e - l * n;
-        C s;
-        if (k < Kh) {
-            s = in[l * Kh + k];
-        } else {
-            s = in[l * Kh + (n - k)];
-            s.y = -s.y;
+    for (int e = threadIdx.x; e < np2 * n; e += blockDim.x) {
+        int p = e / n, k = e - p * n;
+        bool upper = k >= Kh;
+        int kk = upper ? n - k : k;
+        C A = in[(long long)(2 * p) * Kh + kk];
+        C B = (2 * p + 1 < nl) ? in[(long long)(2 * p + 1) * Kh + kk] : Cx<C>::mk((T)0, (T)0);
+        if (upper) {
+            A.y = -A.y;
+            B.y = -B.y;
         }
-        a[e] = s;
+        a[e] = Cx<C>::mk(A.x - B.y, A.y + B.x);
     }
     __syncthreads();
-    C *res = fft_lines(a, b, n, nl, F.rad[2], F.np[2], tw_table<C>(v, F.tw[2]), +1);
+    C *res = fft_lines(a, b, n, np2, F.rad[2], F.np[2], tw_table<C>(v, F.tw[2]), +1);
     T *out = static_cast<T *>(v.grid_real) + F.roff + (long long)l0 * n;
-    for (int e = threadIdx.x; e < nl * n; e += blockDim.x) out[e] = res[e].x;
+    for (int e = threadIdx.x; e < np2 * n; e += blockDim.x) {
+        int p = e / n, z = e - p * n;
+        C r = res[e];
+        out[(long long)(2 * p) * n + z] = r.x;
+        if (2 * p + 1 < nl) out[(long long)(2 * p + 1) * n + z] = r.y;
+    }
 }
 
 template <typename C, typename Acc, typename ET>
@@ -309,7 +342,7 @@ void fft_plan_build(FftPlan &p, int mixed) {
         for (int u = 0; u < F.K[1] * chunks; ++u) x.push_back({s, u});
     }
     size_t csz = mixed ? sizeof(float2) : sizeof(double2);
-    p.smem_z = 2 * (size_t)p.zlines * p.kmax * csz;
+    p.smem_z = 2 * (size_t)(p.zlines / 2) * p.kmax * csz;
     p.smem_y = 2 * (size_t)p.cols * p.kmax * csz;
     p.smem_x = p.smem_y;
     cudaMalloc(&p.dsys, sizeof(FftSysDev) * p.S);

@@ -173,113 +173,6 @@ __global__ void k_derive(DevView v, int gated) {
     v.xref[2 * v.N + s] = z;
 }
 
-// One warp per atom i: scan the 5x5x5 block of cells around i's cell (cells
-// are >= (cutoff + skin)/2 wide), skipping cells whose box is farther than
-// the list radius from i, and append every j != i within the list radius
-// that is not in i's exclusion set.  Entry = slot j | (cell-image code << 25);
-// dtab[code] is the FP32 displacement that turns j's cell-relative offset
-// into i's frame, so the pair kernel needs no minimum-image arithmetic.
-__global__ void __launch_bounds__(256) k_build(DevView v) {
-    const unsigned full = 0xffffffffu;
-    if (!v.flags->rebuild) return;
-    int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    int lane = threadIdx.x & 31;
-    if (i >= v.N) return;
-    int sys = v.sys_of[i];
-    const SysDev &S = v.sys[sys];
-    if (!S.nb_on) {
-        if (lane == 0) v.ncount[i] = 0;
-        return;
-    }
-    int c3 = v.cell3[i];
-    int ci[3] = {c3 & 1023, (c3 >> 10) & 1023, (c3 >> 20) & 1023};
-    float pix, piy, piz;
-    if (v.mixed) {
-        float4 p = v.pf[i];
-        pix = p.x;
-        piy = p.y;
-        piz = p.z;
-    } else {
-        double px = v.x[i], py = v.y[i], pz = v.z[i];
-        pix = (float)min_image(px - (S.lb[0] + ci[0] * S.cs[0]), S.L[0], S.halfL[0]);
-        piy = (float)min_image(py - (S.lb[1] + ci[1] * S.cs[1]), S.L[1], S.halfL[1]);
-        piz = (float)min_image(pz - (S.lb[2] + ci[2] * S.cs[2]), S.L[2], S.halfL[2]);
-    }
-    float pi3[3] = {pix, piy, piz};
-    float csf[3] = {(float)S.cs[0], (float)S.cs[1], (float)S.cs[2]};
-    int oi = v.orig[i];
-    int e0 = v.excl_off[oi];
-    int ne = v.excl_off[oi + 1] - e0;
-    int my_ex = lane < ne ? v.excl_lst[e0 + lane] : -1;
-    int nfast = ne < 32 ? ne : 32;
-    // FP32 positions of the list test carry ~1e-7 nm error; the margin keeps
-    // every pair the exact FP64 test could accept.
-    float rl2 = S.rlist2f * 1.0001f + 1e-6f;
-    int count = 0;
-    size_t base = (size_t)i * v.stride;
-    for (int ox = -2; ox <= 2; ++ox) {
-        float gx = ox > 0 ? ox * csf[0] - pi3[0] : (ox < 0 ? pi3[0] - (ox + 1) * csf[0] : 0.f);
-        gx = fmaxf(gx, 0.f);
-        int nx = wrapi(ci[0] + ox, S.nc[0]);
-        for (int oy = -2; oy <= 2; ++oy) {
-            float gy = oy > 0 ? oy * csf[1] - pi3[1] : (oy < 0 ? pi3[1] - (oy + 1) * csf[1] : 0.f);
-            gy = fmaxf(gy, 0.f);
-            int ny = wrapi(ci[1] + oy, S.nc[1]);
-            for (int oz = -2; oz <= 2; ++oz) {
-                float gz = oz > 0 ? oz * csf[2] - pi3[2] : (oz < 0 ? pi3[2] - (oz + 1) * csf[2] : 0.f);
-                gz = fmaxf(gz, 0.f);
-                if (gx * gx + gy * gy + gz * gz > rl2) continue;  // uniform across the warp
-                int nz = wrapi(ci[2] + oz, S.nc[2]);
-                int code = (ox + 2) * 25 + (oy + 2) * 5 + (oz + 2);
-                float4 D = v.dtab[sys * 128 + code];
-                int key = S.cell_off + (nx * S.nc[1] + ny) * S.nc[2] + nz;
-                int a = v.cell_start[key], b = v.cell_start[key + 1];
-                for (int j0 = a; j0 < b; j0 += 32) {
-                    int j = j0 + lane;
-                    bool cand = false;
-                    if (j < b && j != i) {
-                        float dx, dy, dz;
-                        if (v.mixed) {
-                            float4 pj = v.pf[j];
-                            dx = pix - pj.x + D.x;
-                            dy = piy - pj.y + D.y;
-                            dz = piz - pj.z + D.z;
-                        } else {
-                            int cj = v.cell3[j];
-                            int cjx = cj & 1023, cjy = (cj >> 10) & 1023, cjz = (cj >> 20) & 1023;
-                            float qx = (float)min_image(v.x[j] - (S.lb[0] + cjx * S.cs[0]), S.L[0], S.halfL[0]);
-                            float qy = (float)min_image(v.y[j] - (S.lb[1] + cjy * S.cs[1]), S.L[1], S.halfL[1]);
-                            float qz = (float)min_image(v.z[j] - (S.lb[2] + cjz * S.cs[2]), S.L[2], S.halfL[2]);
-                            dx = pix - qx + D.x;
-                            dy = piy - qy + D.y;
-                            dz = piz - qz + D.z;
-                        }
-                        float r2 = dx * dx + dy * dy + dz * dz;
-                        cand = r2 < rl2;
-                    }
-                    if (!__any_sync(full, cand)) continue;
-                    int oj = cand ? v.orig[j] : -2;
-                    bool ex = false;
-                    for (int e = 0; e < nfast; ++e) ex |= (__shfl_sync(full, my_ex, e) == oj);
-                    if (ne > 32 && cand)
-                        for (int e = 32; e < ne; ++e) ex |= (v.excl_lst[e0 + e] == oj);
-                    bool ok = cand && !ex;
-                    unsigned m = __ballot_sync(full, ok);
-                    if (ok) {
-                        int pos = count + __popc(m & ((1u << lane) - 1u));
-                        if (pos < v.stride) v.nlist[base + pos] = (uint32_t)j | ((uint32_t)code << 25);
-                    }
-                    count += __popc(m);
-                }
-            }
-        }
-    }
-    if (lane == 0) {
-        v.ncount[i] = count < v.stride ? count : v.stride;
-        if (count > v.stride) atomicOr(&v.flags->error, ERR_NLIST_OVERFLOW);
-    }
-}
-
 __global__ void k_remap(DevView v) {
     if (!v.flags->rebuild) return;
     int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -329,7 +222,7 @@ void launch_nlist_rebuild(const DevView &v, cudaStream_t st) {
     k_derive<<<blocks(v.N, 256), 256, 0, st>>>(v, 1);
     long long nt = (long long)v.nb + v.na + v.nt + v.nex;
     if (nt > 0) k_remap<<<blocks(nt, 256), 256, 0, st>>>(v);
-    k_build<<<blocks((long long)v.N * 32, 256), 256, 0, st>>>(v);
+    launch_build(v, st);
 }
 
 }  // namespace nxm

@@ -1,0 +1,458 @@
+// Neighbour-list build and real-space pair forces on shared-memory tiles.
+//
+// One block per group of consecutive cells (nxm_hood.cuh): the block stages
+// the group's neighbourhood once, then each warp takes atoms of the group.
+//
+// Physics follows NonbondedForce::DirectForcesAndEnergy
+// (core/baseline/src/Forces/NonbondedForce.cpp:530-585): sigma_ij =
+// sigma_i/2 + sigma_j/2, eps_ij = (2 sqrt eps_i)(2 sqrt eps_j), no LJ shift,
+// no dispersion correction.  The optional switching function is applied per
+// pair (the reference never resets its switch state between pairs, :541;
+// that order-dependent carry-over is not reproduced).  Pair membership is
+// decided exactly as the reference's list does (NeighborList.cpp:106-116):
+// FP64 single-shift minimum image (PeriodicBoundaryCondition.cpp:93-104),
+// r^2 < cutoff^2.  The list holds a superset (cutoff + skin, FP32 test with
+// a safety margin); in mixed mode the FP32 r^2 settles every pair except
+// those within 1e-5 relative of the cutoff, which are re-tested in FP64.
+#include "nxm_hood.cuh"
+#include "nxm_view.h"
+
+namespace nxm {
+
+// r^2 of the pair exactly as the reference forms it: d = p_j - p_i with one
+// shift per component, then (dx*dx + dy*dy) + dz*dz with no fused multiply-add.
+__device__ __forceinline__ double exact_r2(const DevView &v, const SysDev &S, int i, int j) {
+    double dx = min_image(__dsub_rn(v.x[j], v.x[i]), S.L[0], S.halfL[0]);
+    double dy = min_image(__dsub_rn(v.y[j], v.y[i]), S.L[1], S.halfL[1]);
+    double dz = min_image(__dsub_rn(v.z[j], v.z[i]), S.L[2], S.halfL[2]);
+    return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+__device__ __forceinline__ void offset_in_cell(const DevView &v, const SysDev &S, int s, int c3, float o[3]) {
+    int c[3] = {c3 & 1023, (c3 >> 10) & 1023, (c3 >> 20) & 1023};
+    double p[3] = {v.x[s], v.y[s], v.z[s]};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) o[d] = (float)min_image(p[d] - (S.lb[d] + c[d] * S.cs[d]), S.L[d], S.halfL[d]);
+}
+
+// Atom i's position in the frame of the group's first cell.
+__device__ __forceinline__ void i_in_group_frame(const DevView &v, const SysDev &S, int i, int cz_first, float p[3]) {
+    int c3 = v.cell3[i];
+    float gz = (float)(hood_wrap(((c3 >> 20) & 1023) - cz_first, S.nc[2])) * (float)S.cs[2];
+    if (v.mixed) {
+        float4 q = v.pf[i];
+        p[0] = q.x;
+        p[1] = q.y;
+        p[2] = q.z + gz;
+    } else {
+        offset_in_cell(v, S, i, c3, p);
+        p[2] += gz;
+    }
+}
+
+// Stage the group's neighbourhood: positions shifted into the group frame
+// (.w = scaled charge in mixed mode), LJ parameters (mixed), and for the
+// build also slots and original indices.
+template <bool BUILD, bool MIXED>
+__device__ int stage(const DevView &v, const SysDev &S, int sys, int c3_first, int g, float4 *s_q, float2 *s_lj,
+                     int *s_slot, int *s_orig, HoodSpan *spans, int *s_n) {
+    int n = hood_spans(v, S, c3_first, g, spans, s_n);
+    int nsp = min(s_n[1], kMaxSpans);
+    if (n > v.hood_cap || s_n[1] > kMaxSpans) {
+        if (threadIdx.x == 0) atomicOr(&v.flags->error, ERR_NLIST_OVERFLOW);
+        return -1;
+    }
+    const float4 *dt = v.dtab + sys * kDtabStride;
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int sp = warp; sp < nsp; sp += nw) {
+        HoodSpan h = spans[sp];
+        for (int t = lane; t < h.count; t += 32) {
+            int j = h.start + t, k = h.offset + t;
+            int cj = v.cell3[j];
+            float4 D = __ldg(dt + h.code0 + (((cj >> 20) & 1023) - h.cz0));
+            if (BUILD || MIXED) {
+                float q3[3];
+                float w = 0.f;
+                if (MIXED) {
+                    float4 p = v.pf[j];
+                    q3[0] = p.x;
+                    q3[1] = p.y;
+                    q3[2] = p.z;
+                    w = p.w;
+                } else {
+                    offset_in_cell(v, S, j, cj, q3);
+                }
+                s_q[k] = make_float4(q3[0] - D.x, q3[1] - D.y, q3[2] - D.z, w);
+            }
+            if (MIXED && !BUILD) s_lj[k] = v.ljf[j];
+            if (BUILD) {
+                s_slot[k] = j;
+                s_orig[k] = v.orig[j];
+            }
+        }
+    }
+    __syncthreads();
+    return n;
+}
+
+// List layout: each 256-entry chunk of an atom's list is stored transposed,
+// entry p of the chunk at position 8 * (p mod 32) + p / 32, so that lane L
+// of a warp fetches entries L, L+32, ..., L+224 with one 16-byte load.
+__device__ __forceinline__ int list_pos(int p) { return (p & ~255) | ((p & 31) << 3) | ((p >> 5) & 7); }
+
+// ------------------------------------------------------------------ build
+
+// Each warp takes atoms of the group; every staged atom within the list
+// radius that is not i itself and not excluded is appended to i's list as
+// its 16-bit tile index (ballot compaction: deterministic order).
+__global__ void __launch_bounds__(kHoodWarps * 32) k_build(DevView v) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    if (!v.flags->rebuild) return;
+    const unsigned full = 0xffffffffu;
+    CellGroup G = v.groups[blockIdx.x];
+    int a0 = v.cell_start[G.cell], a1 = v.cell_start[G.cell + G.ncell];
+    if (a0 == a1) return;
+    const SysDev &S = v.sys[G.sys];
+    if (!S.nb_on) {
+        for (int i = a0 + threadIdx.x; i < a1; i += blockDim.x) v.ncount[i] = 0;
+        return;
+    }
+    int cap = v.hood_cap;
+    float4 *s_q = reinterpret_cast<float4 *>(smem);
+    int *s_slot = reinterpret_cast<int *>(s_q + cap);
+    int *s_orig = s_slot + cap;
+    HoodSpan *spans = reinterpret_cast<HoodSpan *>(s_orig + cap);
+    int *s_n = reinterpret_cast<int *>(spans + kMaxSpans);
+    int c3f = v.cell3[a0];
+    int n = v.mixed ? stage<true, true>(v, S, G.sys, c3f, G.ncell, s_q, nullptr, s_slot, s_orig, spans, s_n)
+                    : stage<true, false>(v, S, G.sys, c3f, G.ncell, s_q, nullptr, s_slot, s_orig, spans, s_n);
+    if (n < 0) return;
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    float rl2 = S.rlist2f * 1.0001f + 1e-6f;
+    int czf = (c3f >> 20) & 1023;
+    for (int i = a0 + warp; i < a1; i += nw) {
+        float pi3[3];
+        i_in_group_frame(v, S, i, czf, pi3);
+        int oi = v.orig[i];
+        int e0 = v.excl_off[oi];
+        int ne = v.excl_off[oi + 1] - e0;
+        int my_ex = lane < ne ? v.excl_lst[e0 + lane] : -1;
+        int nfast = ne < 32 ? ne : 32;
+        // index window of the exclusion partners: candidates outside it need
+        // no membership test
+        int ex_lo = ne ? v.excl_lst[e0] : 1, ex_hi = ne ? v.excl_lst[e0 + ne - 1] : 0;
+        int count = 0;
+        uint16_t *out = v.nl16 + (size_t)i * v.stride;
+        for (int k0 = 0; k0 < n; k0 += 32) {
+            int k = k0 + lane;
+            bool cand = false;
+            if (k < n) {
+                float4 q = s_q[k];
+                float dx = pi3[0] - q.x, dy = pi3[1] - q.y, dz = pi3[2] - q.z;
+                cand = dx * dx + dy * dy + dz * dz < rl2 && s_slot[k] != i;
+            }
+            if (!__any_sync(full, cand)) continue;
+            int oj = cand ? s_orig[k] : -2;
+            bool ex = false;
+            if (__any_sync(full, cand && oj >= ex_lo && oj <= ex_hi)) {
+                for (int e = 0; e < nfast; ++e) ex |= (__shfl_sync(full, my_ex, e) == oj);
+                if (ne > 32 && cand)
+                    for (int e = 32; e < ne; ++e) ex |= (v.excl_lst[e0 + e] == oj);
+            }
+            bool ok = cand && !ex;
+            unsigned m = __ballot_sync(full, ok);
+            if (ok) {
+                int pos = count + __popc(m & ((1u << lane) - 1u));
+                if (pos < v.stride) out[list_pos(pos)] = (uint16_t)k;
+            }
+            count += __popc(m);
+        }
+        if (lane == 0) {
+            v.ncount[i] = count < v.stride ? count : v.stride;
+            if (count > v.stride) atomicOr(&v.flags->error, ERR_NLIST_OVERFLOW);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ pairs
+
+struct PairPrm {
+    float alpha, sw, cut;
+    int use_sw;
+};
+
+// FP32 force (and energy) of one pair inside the cutoff, accumulated into
+// the lane's partial sums (NonbondedForce.cpp:559-581 in single precision).
+template <bool ENERGY>
+__device__ __forceinline__ void pair_mixed(float dx, float dy, float dz, float r2, float qq, float sg, float eps,
+                                           const PairPrm &P, float &fx, float &fy, float &fz, float &ec,
+                                           float &ev) {
+    float rinv = rsqrtf(r2);
+    float rinv2 = rinv * rinv;
+    float r = r2 * rinv;
+    float xa = P.alpha * r;
+    float ex = __expf(-xa * xa);
+    float erfcv = ex * erfcx_fit(fast_rcp(fmaf(0.4f, xa, 1.0f)));
+    float dEdR = qq * rinv * rinv2 * fmaf((float)kTwoOverSqrtPi * xa, ex, erfcv);
+    float s2 = sg * sg * rinv2;
+    float s6 = s2 * s2 * s2;
+    float evdw = eps * (s6 - 1.0f) * s6;
+    float sw = 1.0f;
+    if (P.use_sw && r > P.sw) {
+        float w = P.cut - P.sw;
+        float t = (r - P.sw) / w;
+        sw = 1.0f + t * t * t * (-10.0f + t * (15.0f - t * 6.0f));
+        float dsw = t * t * (-30.0f + t * (60.0f - t * 30.0f)) / w;
+        dEdR -= evdw * dsw * rinv;
+    }
+    dEdR = fmaf(sw * eps * (12.0f * s6 - 6.0f) * s6, rinv2, dEdR);
+    fx = fmaf(dx, dEdR, fx);
+    fy = fmaf(dy, dEdR, fy);
+    fz = fmaf(dz, dEdR, fz);
+    if (ENERGY) {
+        ec = fmaf(qq * rinv, erfcv, ec);
+        ev = fmaf(sw, evdw, ev);
+    }
+}
+
+// Mixed precision: each lane keeps two list entries in flight; j comes from
+// the staged tile.
+template <bool ENERGY>
+__global__ void __launch_bounds__(kHoodWarps * 32) k_pairs_mixed(DevView v) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const unsigned full = 0xffffffffu;
+    CellGroup G = v.groups[blockIdx.x];
+    int a0 = v.cell_start[G.cell], a1 = v.cell_start[G.cell + G.ncell];
+    if (a0 == a1) return;
+    const SysDev &S = v.sys[G.sys];
+    if (!S.nb_on) return;
+    int cap = v.hood_cap;
+    float4 *s_q = reinterpret_cast<float4 *>(smem);
+    float2 *s_lj = reinterpret_cast<float2 *>(s_q + cap);
+    HoodSpan *spans = reinterpret_cast<HoodSpan *>(s_lj + cap);
+    int *s_n = reinterpret_cast<int *>(spans + kMaxSpans);
+    int c3f = v.cell3[a0];
+    int n = stage<false, true>(v, S, G.sys, c3f, G.ncell, s_q, s_lj, nullptr, nullptr, spans, s_n);
+    if (n < 0) return;
+    int nsp = s_n[1];
+    int czf = (c3f >> 20) & 1023;
+    const float lo = S.cut2f_lo, hi = S.cut2f_hi;
+    const PairPrm P{S.alphaf, S.sw_distf, S.cutofff, S.use_switch};
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    float ec = 0.f, ev = 0.f;
+    for (int i = a0 + warp; i < a1; i += nw) {
+        float pi3[3];
+        i_in_group_frame(v, S, i, czf, pi3);
+        const float qi = v.pf[i].w;
+        const float2 li = v.ljf[i];
+        const int cnt = v.ncount[i];
+        const uint4 *lst4 = reinterpret_cast<const uint4 *>(v.nl16 + (size_t)i * v.stride) + lane;
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+        uint4 cur = cnt > 0 ? __ldg(lst4) : make_uint4(0, 0, 0, 0);
+        for (int c0 = 0; c0 < cnt; c0 += 256) {
+            // this lane's entries c0 + lane + 32u, u = 0..7, and the next chunk in flight
+            uint4 nxt = c0 + 256 < cnt ? __ldg(lst4 + (c0 + 256) / 8) : make_uint4(0, 0, 0, 0);
+            uint32_t wds[4] = {cur.x, cur.y, cur.z, cur.w};
+#pragma unroll
+            for (int u = 0; u < 8; u += 2) {
+            int k0 = c0 + lane + 32 * u, k1 = k0 + 32;
+            bool v0 = k0 < cnt, v1 = k1 < cnt;
+            int t0 = v0 ? (int)(wds[u >> 1] & 0xffffu) : 0;
+            int t1 = v1 ? (int)(wds[u >> 1] >> 16) : 0;
+            float4 p0 = s_q[t0], p1 = s_q[t1];
+            float2 l0 = s_lj[t0], l1 = s_lj[t1];
+            float dx0 = pi3[0] - p0.x, dy0 = pi3[1] - p0.y, dz0 = pi3[2] - p0.z;
+            float dx1 = pi3[0] - p1.x, dy1 = pi3[1] - p1.y, dz1 = pi3[2] - p1.z;
+            float r20 = v0 ? dx0 * dx0 + dy0 * dy0 + dz0 * dz0 : 1e30f;
+            float r21 = v1 ? dx1 * dx1 + dy1 * dy1 + dz1 * dz1 : 1e30f;
+            bool in0 = r20 < lo, in1 = r21 < lo;
+            bool b0 = !in0 && r20 < hi, b1 = !in1 && r21 < hi;
+            if (__any_sync(full, b0 || b1)) {
+                // within 1e-5 of the cutoff: decide in FP64 exactly as the reference
+                if (b0) in0 = exact_r2(v, S, i, hood_slot(spans, nsp, t0)) < S.cut2;
+                if (b1) in1 = exact_r2(v, S, i, hood_slot(spans, nsp, t1)) < S.cut2;
+            }
+            if (in0) pair_mixed<ENERGY>(dx0, dy0, dz0, r20, qi * p0.w, li.x + l0.x, li.y * l0.y, P, fx, fy, fz, ec, ev);
+            if (in1) pair_mixed<ENERGY>(dx1, dy1, dz1, r21, qi * p1.w, li.x + l1.x, li.y * l1.y, P, fx, fy, fz, ec, ev);
+            }
+            cur = nxt;
+        }
+        fx = warp_sum(fx);
+        fy = warp_sum(fy);
+        fz = warp_sum(fz);
+        if (lane == 0) {
+            acc_add(static_cast<long long *>(v.fx) + i, fx);
+            acc_add(static_cast<long long *>(v.fy) + i, fy);
+            acc_add(static_cast<long long *>(v.fz) + i, fz);
+        }
+    }
+    if (ENERGY) {
+        // each pair sits in both partners' lists
+        energy_add(v.E, G.sys, E_COUL, 0.5 * (double)ec);
+        energy_add(v.E, G.sys, E_VDW, 0.5 * (double)ev);
+    }
+}
+
+// FP64 form: the same list; every pair in double precision from the FP64
+// positions with the reference's minimum image (NonbondedForce.cpp:548-581).
+template <bool ENERGY>
+__global__ void __launch_bounds__(kHoodWarps * 32) k_pairs_fp64(DevView v) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    CellGroup G = v.groups[blockIdx.x];
+    int a0 = v.cell_start[G.cell], a1 = v.cell_start[G.cell + G.ncell];
+    if (a0 == a1) return;
+    const SysDev &S = v.sys[G.sys];
+    if (!S.nb_on) return;
+    HoodSpan *spans = reinterpret_cast<HoodSpan *>(smem);
+    int *s_n = reinterpret_cast<int *>(spans + kMaxSpans);
+    int n = hood_spans(v, S, v.cell3[a0], G.ncell, spans, s_n);
+    if (n > v.hood_cap || s_n[1] > kMaxSpans) {
+        if (threadIdx.x == 0) atomicOr(&v.flags->error, ERR_NLIST_OVERFLOW);
+        return;
+    }
+    int nsp = s_n[1];
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    double ec = 0, ev = 0;
+    for (int i = a0 + warp; i < a1; i += nw) {
+        double xi = v.x[i], yi = v.y[i], zi = v.z[i];
+        double qi = v.qs[i];
+        double2 li = v.ljd[i];
+        int cnt = v.ncount[i];
+        const uint16_t *lst = v.nl16 + (size_t)i * v.stride;
+        double fx = 0, fy = 0, fz = 0;
+        for (int k = lane; k < cnt; k += 32) {
+            int j = hood_slot(spans, nsp, lst[list_pos(k)]);
+            if (!(exact_r2(v, S, i, j) < S.cut2)) continue;
+            // deltaR = minimumImageVector(p_i, p_j) (NonbondedForce.cpp:548)
+            double dx = min_image(xi - v.x[j], S.L[0], S.halfL[0]);
+            double dy = min_image(yi - v.y[j], S.L[1], S.halfL[1]);
+            double dz = min_image(zi - v.z[j], S.L[2], S.halfL[2]);
+            double r = sqrt(dx * dx + dy * dy + dz * dz);
+            double rinv = 1.0 / r;
+            double sw = 1.0, dsw = 0.0;
+            if (S.use_switch && r > S.sw_dist) {
+                double t = (r - S.sw_dist) / (S.cutoff - S.sw_dist);
+                sw = 1 + t * t * t * (-10 + t * (15 - t * 6));
+                dsw = t * t * (-30 + t * (60 - t * 30)) / (S.cutoff - S.sw_dist);
+            }
+            double xa = S.alpha * r;
+            double qq = qi * v.qs[j];
+            double erfcv = erfc(xa);
+            double dEdR = qq * rinv * rinv * rinv * (erfcv + 2 * xa * exp(-xa * xa) / kSqrtPi);
+            double2 lj = v.ljd[j];
+            double sg = li.x + lj.x;
+            double s2 = sg * rinv;
+            s2 *= s2;
+            double s6 = s2 * s2 * s2;
+            double eps = li.y * lj.y;
+            dEdR += sw * eps * (12.0 * s6 - 6.0) * s6 * rinv * rinv;
+            double evdw = eps * (s6 - 1.0) * s6;
+            if (S.use_switch) {
+                dEdR -= evdw * dsw * rinv;
+                evdw *= sw;
+            }
+            fx += dx * dEdR;
+            fy += dy * dEdR;
+            fz += dz * dEdR;
+            if (ENERGY) {
+                ec += qq * rinv * erfcv;
+                ev += evdw;
+            }
+        }
+        fx = warp_sum(fx);
+        fy = warp_sum(fy);
+        fz = warp_sum(fz);
+        if (lane == 0) {
+            atomicAdd(static_cast<double *>(v.fx) + i, fx);
+            atomicAdd(static_cast<double *>(v.fy) + i, fy);
+            atomicAdd(static_cast<double *>(v.fz) + i, fz);
+        }
+    }
+    if (ENERGY) {
+        energy_add(v.E, G.sys, E_COUL, 0.5 * ec);
+        energy_add(v.E, G.sys, E_VDW, 0.5 * ev);
+    }
+}
+
+// ---- test support: the neighbour pair set within the cutoff, exactly as
+// the reference decides it, as (larger, smaller) original indices.
+__global__ void k_collect(DevView v, int sys_sel, int *out, long long cap, unsigned long long *n_out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    CellGroup G = v.groups[blockIdx.x];
+    if (G.sys != sys_sel) return;
+    int a0 = v.cell_start[G.cell], a1 = v.cell_start[G.cell + G.ncell];
+    if (a0 == a1) return;
+    const SysDev &S = v.sys[G.sys];
+    if (!S.nb_on) return;
+    HoodSpan *spans = reinterpret_cast<HoodSpan *>(smem);
+    int *s_n = reinterpret_cast<int *>(spans + kMaxSpans);
+    hood_spans(v, S, v.cell3[a0], G.ncell, spans, s_n);
+    if (s_n[1] > kMaxSpans) return;
+    int nsp = s_n[1];
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int i = a0 + warp; i < a1; i += nw) {
+        int oi = v.orig[i];
+        int cnt = v.ncount[i];
+        for (int k = lane; k < cnt; k += 32) {
+            int j = hood_slot(spans, nsp, v.nl16[(size_t)i * v.stride + list_pos(k)]);
+            int oj = v.orig[j];
+            if (oi <= oj) continue;
+            if (!(exact_r2(v, S, i, j) < S.cut2)) continue;
+            unsigned long long p = atomicAdd(n_out, 1ull);
+            if ((long long)p < cap) {
+                out[2 * p] = oi - S.atom_off;
+                out[2 * p + 1] = oj - S.atom_off;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ launch
+
+static size_t tail_bytes() { return kMaxSpans * sizeof(HoodSpan) + 4 * sizeof(int); }
+static size_t smem_build(int cap) { return (size_t)cap * (sizeof(float4) + 2 * sizeof(int)) + tail_bytes(); }
+static size_t smem_pairs(int cap, int mixed) {
+    return mixed ? (size_t)cap * (sizeof(float4) + sizeof(float2)) + tail_bytes() : tail_bytes();
+}
+
+void tiles_set_smem(int cap) {
+    int b = (int)smem_build(cap), m = (int)smem_pairs(cap, 1);
+    cudaFuncSetAttribute(k_build, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(k_pairs_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_pairs_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+}
+
+void launch_build(const DevView &v, cudaStream_t st) {
+    if (v.ngroups) k_build<<<v.ngroups, kHoodWarps * 32, smem_build(v.hood_cap), st>>>(v);
+}
+
+void launch_pairs(const DevView &v, int energy, cudaStream_t st) {
+    if (v.N == 0 || v.ngroups == 0) return;
+    int g = v.ngroups, t = kHoodWarps * 32;
+    size_t sm = smem_pairs(v.hood_cap, v.mixed);
+    if (v.mixed) {
+        if (energy)
+            k_pairs_mixed<true><<<g, t, sm, st>>>(v);
+        else
+            k_pairs_mixed<false><<<g, t, sm, st>>>(v);
+    } else {
+        if (energy)
+            k_pairs_fp64<true><<<g, t, sm, st>>>(v);
+        else
+            k_pairs_fp64<false><<<g, t, sm, st>>>(v);
+    }
+}
+
+long long launch_collect_pairs(const DevView &v, int sys, int *out_pairs, long long cap, cudaStream_t st) {
+    unsigned long long *dn;
+    cudaMallocAsync(&dn, sizeof(unsigned long long), st);
+    cudaMemsetAsync(dn, 0, sizeof(unsigned long long), st);
+    k_collect<<<v.ngroups, kHoodWarps * 32, tail_bytes(), st>>>(v, sys, out_pairs, cap, dn);
+    unsigned long long n = 0;
+    cudaMemcpyAsync(&n, dn, sizeof(n), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    cudaFreeAsync(dn, st);
+    return (long long)n;
+}
+
+}  // namespace nxm

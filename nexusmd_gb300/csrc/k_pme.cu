@@ -8,6 +8,8 @@
 // weights and derivatives follow computeBSplineParameters (:144-182); the
 // spread is :220-260 and the gather :407-461.  In mixed mode the weights are
 // FP32 and the grid is summed as int64 fixed point (bit-reproducible).
+#include <algorithm>
+
 #include "nxm_fft.h"
 #include "nxm_view.h"
 
@@ -152,6 +154,8 @@ __global__ void __launch_bounds__(128) k_gather(DevView v, const FftSysDev *fs) 
     acc_add(static_cast<Acc_ *>(v.fy) + s, -(q * (fy * (R)(F.K[1] * S.invL[1]))));
     acc_add(static_cast<Acc_ *>(v.fz) + s, -(q * (fz * (R)(F.K[2] * S.invL[2]))));
 }
+
+void spread_set_smem(int) {}
 
 void launch_spread(const DevView &v, const FftPlan &plan, cudaStream_t st) {
     int nb = (v.N + 127) / 128;

@@ -32,6 +32,9 @@ constexpr int kOrder = 5;       // PME B-spline order (NonbondedForce.cpp:474)
 constexpr int kCodeBits = 7;    // list entry = slot (25 bits) | cell-image code (7 bits)
 constexpr uint32_t kSlotMask = (1u << 25) - 1u;
 constexpr int kMaxExclFast = 32;
+// cell-image displacement table per system: 5 (x) * 5 (y) * 12 (z) codes
+constexpr int kDtabStride = 320;
+constexpr int kMaxGroupCells = 8;  // cells per group of the tile kernels (5*5*(8+4) = 300 codes)
 
 // Energy slots per system.
 enum EnergyTerm {

@@ -189,7 +189,8 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     long long roff = 0, coff = 0;
     int tw_total = 0;
     double skin = opt.skin > 0 ? opt.skin : 0.0;
-    int stride = 0;
+    int stride = 0, hood_cap = 0;
+    std::vector<int> group_g(S, 1);
     for (int s = 0; s < S; ++s) {
         const HostSystem &h = systems[s];
         SysDev &D = sysd_[s];
@@ -289,10 +290,25 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         double expect = 4.0 / 3.0 * kPi * H.rlist * H.rlist * H.rlist * h.n / vol;
         int cap = (int)(1.6 * expect + 64);
         stride = std::max(stride, cap);
+        // tile kernels: groups of G cells along z; the staged neighbourhood
+        // holds 5 x 5 x (G + 4) cells.  The largest G whose neighbourhood
+        // (with 30% headroom over the mean density) stays within ~100 KB of
+        // shared memory, at most nz - 4 so no cell appears twice.
+        double cell_atoms = sysd_[s].cs[0] * sysd_[s].cs[1] * sysd_[s].cs[2] * h.n / vol;
+        int gmax = std::max(1, std::min(kMaxGroupCells, sysd_[s].nc[2] - 4));
+        int G = 1;
+        for (int g = gmax; g >= 1; --g)
+            if (25.0 * (g + 4) * cell_atoms * 1.3 + 128 <= 4200.0) {
+                G = g;
+                break;
+            }
+        group_g[s] = G;
+        int hood = (int)(25.0 * (G + 4) * cell_atoms * 1.3 + 128);
+        hood_cap = std::max(hood_cap, hood);
         off += h.n;
     }
     if (opt.max_neighbors > 0) stride = opt.max_neighbors;
-    stride = (stride + 31) / 32 * 32;
+    stride = (stride + 255) / 256 * 256;  // whole 256-entry chunks (transposed list layout)
 
     // ---- device memory
     cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking);
@@ -329,12 +345,36 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     v_.cell_start = dalloc<int>(cell_off + 1);
     v_.cell_fill = dalloc<int>(cell_off + 1);
     v_.new_orig = dalloc<int>(N_);
-    v_.nlist = dalloc<uint32_t>((size_t)N_ * stride);
+    hood_cap = (hood_cap + 31) / 32 * 32;
+    if (hood_cap > 65535) return "neighbourhood too dense for 16-bit list entries";
+    v_.hood_cap = hood_cap;
+    v_.nl16 = dalloc<uint16_t>((size_t)N_ * stride);
+    {
+        // groups of G consecutive cells along each z-row of every system
+        std::vector<CellGroup> gr;
+        for (int s = 0; s < S; ++s) {
+            const SysDev &D = sysd_[s];
+            int G = group_g[s];
+            for (int cx = 0; cx < D.nc[0]; ++cx)
+                for (int cy = 0; cy < D.nc[1]; ++cy)
+                    for (int cz = 0; cz < D.nc[2]; cz += G) {
+                        CellGroup g;
+                        g.cell = D.cell_off + (cx * D.nc[1] + cy) * D.nc[2] + cz;
+                        g.ncell = std::min(G, D.nc[2] - cz);
+                        g.sys = s;
+                        gr.push_back(g);
+                    }
+        }
+        v_.ngroups = (int)gr.size();
+        v_.groups = dalloc<CellGroup>(gr.size());
+        cudaMemcpy(v_.groups, gr.data(), sizeof(CellGroup) * gr.size(), cudaMemcpyHostToDevice);
+    }
+    tiles_set_smem(hood_cap);
     v_.ncount = dalloc<int>(N_);
-    v_.dtab = dalloc<float4>((size_t)S * 128);
+    v_.dtab = dalloc<float4>((size_t)S * kDtabStride);
     v_.xref = dalloc<double>(3 * (size_t)N_);
     v_.tmp = dalloc<double>(11 * (size_t)N_);
-    if (!v_.nlist || !v_.tmp) return "device allocation failed (neighbour list)";
+    if (!v_.nl16 || !v_.tmp) return "device allocation failed (neighbour list)";
 
     // host staging in original order (slot = original index until the first sort)
     std::vector<int> sys_of(N_), iota(N_);
@@ -370,15 +410,17 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     up(v_.sig, hs.data(), sizeof(double) * N_);
     up(v_.eps, he.data(), sizeof(double) * N_);
 
-    // cell-image displacement table: code (ox,oy,oz) -> -(o . cs)
-    std::vector<float4> dt((size_t)S * 128, make_float4(0, 0, 0, 0));
+    // cell-image displacement table: code ((ox+2)*5 + (oy+2))*12 + (oz+2) -> -(o . cs),
+    // o relative to the first cell of a group (oz from -2 to kMaxGroupCells + 1)
+    std::vector<float4> dt((size_t)S * kDtabStride, make_float4(0, 0, 0, 0));
     for (int s = 0; s < S; ++s)
         for (int ox = -2; ox <= 2; ++ox)
             for (int oy = -2; oy <= 2; ++oy)
-                for (int oz = -2; oz <= 2; ++oz) {
-                    int code = (ox + 2) * 25 + (oy + 2) * 5 + (oz + 2);
-                    dt[(size_t)s * 128 + code] = make_float4((float)(-ox * sysd_[s].cs[0]), (float)(-oy * sysd_[s].cs[1]),
-                                                             (float)(-oz * sysd_[s].cs[2]), 0.f);
+                for (int oz = -2; oz <= kMaxGroupCells + 1; ++oz) {
+                    int code = ((ox + 2) * 5 + (oy + 2)) * (kMaxGroupCells + 4) + (oz + 2);
+                    dt[(size_t)s * kDtabStride + code] =
+                        make_float4((float)(-ox * sysd_[s].cs[0]), (float)(-oy * sysd_[s].cs[1]),
+                                    (float)(-oz * sysd_[s].cs[2]), 0.f);
                 }
     up(v_.dtab, dt.data(), sizeof(float4) * dt.size());
 
@@ -545,6 +587,23 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         // FFT work lists only for systems with nonbonded forces: systems
         // without them keep an empty grid that no block touches
         fft_plan_build(plan_, mixed_);
+        // shared-memory sub-grid of the grouped spread: a group's cells plus
+        // the drift margin on both sides plus the stencil reach, per axis
+        v_.spread_margin = 0.5 * skin + 1e-3;
+        int sp_cap = 0;
+        for (int s = 0; s < S; ++s) {
+            const SysDev &D = sysd_[s];
+            int ncell[3] = {1, 1, group_g[s]};
+            long long vol = 1;
+            for (int d = 0; d < 3; ++d) {
+                double span = ncell[d] * D.cs[d] + 2 * v_.spread_margin;
+                int e = (int)std::ceil(span / D.L[d] * D.K[d]) + 1 + kOrder;
+                vol *= std::min(e, D.K[d]);
+            }
+            sp_cap = (int)std::max<long long>(sp_cap, vol);
+        }
+        v_.spread_cap = std::min(sp_cap, 12 * 1024);  // <= 96 KB; larger groups take the global path
+        spread_set_smem(v_.spread_cap);
     }
     // systems without nonbonded forces: zero their charges in the PME and
     // pair paths by skipping them entirely (no list, no grid)

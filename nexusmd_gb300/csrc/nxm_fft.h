@@ -34,7 +34,7 @@ struct FftPlan {
     std::vector<FftSysDev> hsys;
     FftWork *zwork = nullptr, *ywork = nullptr, *xwork = nullptr;
     int nz = 0, ny = 0, nx = 0;
-    int zlines = 8;     // lines per block in the z passes
+    int zlines = 16;    // real lines per block in the z passes (even)
     int cols = 8;       // z columns per block in the y and x passes
     size_t smem_z = 0, smem_y = 0, smem_x = 0;
     int kmax = 0;

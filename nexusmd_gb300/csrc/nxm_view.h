@@ -9,6 +9,12 @@
 
 namespace nxm {
 
+struct CellGroup {
+    int cell;   // first cell (global index)
+    int ncell;  // consecutive cells along z in the group
+    int sys;
+};
+
 struct DevView {
     int N, S;            // atoms (slots) and systems in the batch
     int mixed;           // 1: FP32 force math + int64 fixed point; 0: FP64 throughout
@@ -32,10 +38,13 @@ struct DevView {
     int total_cells;
     int *cell_key, *cell_count, *cell_start, *cell_fill;
     int *new_orig;
-    uint32_t *nlist;
+    uint16_t *nl16;      // per-atom list of indices into the cell's staged neighbourhood
     int *ncount;
     int stride;
-    float4 *dtab;        // [S][128] cell-image displacement per code
+    struct CellGroup *groups;  // blocks of the tile kernels: runs of cells along z
+    int ngroups;
+    int hood_cap;        // capacity of a staged neighbourhood (atoms)
+    float4 *dtab;        // [S][kDtabStride] cell-image displacement per code
     double *xref;        // [3][N] positions at the last rebuild
     int *excl_off, *excl_lst;  // CSR by original index, partners as original indices
     // scratch used by the permutation
@@ -59,6 +68,8 @@ struct DevView {
     void *grid_cplx;     // half complex grid: float2 / double2
     void *eterm;         // influence function on the half grid: float / double
     void *twiddle;       // float2 / double2 tables, forward sign
+    double spread_margin;  // nm an atom may drift out of its cell between rebuilds
+    int spread_cap;        // points of a cell group's shared-memory sub-grid
     int4 *pme_idx;       // per slot grid base index (x, y, z)
     void *pme_frac;      // per slot fraction: float4 / double4-as-2xdouble2
     // energies, flags, report snapshot (original order, AoS [N][3])
@@ -70,6 +81,8 @@ struct DevView {
 
 // kernel launchers (one per .cu file group)
 void launch_nlist_rebuild(const DevView &v, cudaStream_t st);
+void launch_build(const DevView &v, cudaStream_t st);
+void tiles_set_smem(int hood_cap);
 void launch_derive_inputs(const DevView &v, cudaStream_t st);
 void launch_bonded(const DevView &v, int energy, cudaStream_t st);
 void launch_pairs(const DevView &v, int energy, cudaStream_t st);
@@ -78,6 +91,7 @@ void launch_pme(const DevView &v, const struct FftPlan &plan, int energy, cudaSt
 void launch_spread(const DevView &v, const struct FftPlan &plan, cudaStream_t st);
 void launch_fft_convolve(const DevView &v, const struct FftPlan &plan, int energy, cudaStream_t st);
 void launch_gather(const DevView &v, const struct FftPlan &plan, cudaStream_t st);
+void spread_set_smem(int points);
 void launch_integrate(const DevView &v, double dt, int report, cudaStream_t st);
 void launch_snapshot_forces(const DevView &v, cudaStream_t st);
 void launch_remap_terms(const DevView &v, cudaStream_t st);
