@@ -52,6 +52,14 @@ public:
     // (step 0 and every `interval`-th); `on_report(step)` runs after each.
     template <typename F>
     std::string run_reporting(int nsteps, double dt, int interval, F on_report);
+    // One step; with report != 0 the energies and the x/v/F snapshot of the
+    // step are taken and the call waits for them.
+    std::string advance(double dt, int report) {
+        std::string e = one_step(dt, report);
+        if (!e.empty()) return e;
+        return report ? finish_call() : std::string();
+    }
+    std::string sync() { return finish_call(); }
     std::string get_snapshot(double *x, double *v, double *f);
     std::string get_state(double *x, double *v);
     void energies(int sys, nxm_energies *out) const;

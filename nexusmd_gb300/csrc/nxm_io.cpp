@@ -1,0 +1,325 @@
+// System/state XML readers (core/common/src/SystemXMLParser.cpp:18-196,
+// StateXMLParser.cpp:17-37) and the report writers (core/baseline/src/
+// Reporter.cpp:26-229), producing the same values and the same file bytes.
+#include "nxm_io.h"
+
+#include <cctype>
+#include <cstdio>
+#include <ctime>
+#include <fstream>
+#include <iostream>
+#include <set>
+#include <sstream>
+
+#include "nxm_xml.h"
+
+namespace nxm {
+
+namespace {
+
+bool load(const std::string &path, XmlDoc &doc) {
+    doc = xml_load_file(path);
+    if (!doc.error.empty()) {
+        std::cerr << "XML [" << path << "] parsed with errors, Error description: " << doc.error << "\n";
+        return false;
+    }
+    return true;
+}
+
+const XmlNode *forces_of(const XmlDoc &d) {
+    const XmlNode *sys = d.root.child("System");
+    return sys ? sys->child("Forces") : nullptr;
+}
+
+std::vector<double> masses_of(const XmlDoc &d) {
+    std::vector<double> m;
+    const XmlNode *sys = d.root.child("System");
+    const XmlNode *parts = sys ? sys->child("Particles") : nullptr;
+    if (parts)
+        for (auto *p : parts->children_named("Particle")) m.push_back(p->as_double("mass"));
+    return m;
+}
+
+template <typename F>
+void each_force(const XmlDoc &d, const char *type, F fn) {
+    const XmlNode *fs = forces_of(d);
+    if (!fs) return;
+    for (auto *f : fs->children_named("Force")) {
+        const char *t = f->attr("type");
+        if (t && std::string(t) == type) fn(f);
+    }
+}
+
+std::vector<TorsionP> torsions_of(const XmlDoc &d) {
+    std::vector<TorsionP> out;
+    each_force(d, "PeriodicTorsionForce", [&](const XmlNode *f) {
+        const XmlNode *ts = f->child("Torsions");
+        if (!ts) return;
+        for (auto *t : ts->children_named("Torsion"))
+            out.push_back(TorsionP{t->as_int("p1"), t->as_int("p2"), t->as_int("p3"), t->as_int("p4"),
+                                   t->as_double("k"), t->as_double("phase"), t->as_int("periodicity")});
+    });
+    return out;
+}
+
+std::vector<BondP> bonds_of(const XmlDoc &d) {
+    std::vector<BondP> out;
+    each_force(d, "HarmonicBondForce", [&](const XmlNode *f) {
+        const XmlNode *bs = f->child("Bonds");
+        if (!bs) return;
+        for (auto *b : bs->children_named("Bond"))
+            out.push_back(BondP{b->as_int("p1"), b->as_int("p2"), b->as_double("d"), b->as_double("k")});
+    });
+    return out;
+}
+
+std::vector<AngleP> angles_of(const XmlDoc &d) {
+    std::vector<AngleP> out;
+    each_force(d, "HarmonicAngleForce", [&](const XmlNode *f) {
+        const XmlNode *as = f->child("Angles");
+        if (!as) return;
+        for (auto *a : as->children_named("Angle"))
+            out.push_back(AngleP{a->as_int("p1"), a->as_int("p2"), a->as_int("p3"), a->as_double("a"), a->as_double("k")});
+    });
+    return out;
+}
+
+NbParams nonbonded_of(const XmlDoc &d) {
+    NbParams p;
+    const XmlNode *fs = forces_of(d);
+    if (!fs) {
+        std::cerr << "No Forces node found in the XML.\n";
+        return p;
+    }
+    const XmlNode *f = nullptr;
+    for (auto *c : fs->children_named("Force")) {
+        const char *t = c->attr("type");
+        if (t && std::string(t) == "NonbondedForce") {
+            f = c;
+            break;
+        }
+    }
+    if (!f) {
+        std::cerr << "No NonbondedForce found in the XML.\n";
+        return p;
+    }
+    p.alpha = f->as_double("alpha");
+    p.cutoff = f->as_double("cutoff");
+    p.dispersionCorrection = f->as_int("dispersionCorrection");
+    p.ewaldTolerance = f->as_double("ewaldTolerance");
+    p.exceptionsUsePeriodic = f->as_int("exceptionsUsePeriodic");
+    p.forceGroup = f->as_int("forceGroup");
+    p.includeDirectSpace = f->as_int("includeDirectSpace");
+    p.ljAlpha = f->as_int("ljAlpha");
+    p.ljnx = f->as_int("ljnx");
+    p.ljny = f->as_int("ljny");
+    p.ljnz = f->as_int("ljnz");
+    p.method = f->as_int("method");
+    p.nx = f->as_int("nx");
+    p.ny = f->as_int("ny");
+    p.nz = f->as_int("nz");
+    p.recipForceGroup = f->as_int("recipForceGroup");
+    p.rfDielectric = f->as_double("rfDielectric");
+    p.switchingDistance = f->as_double("switchingDistance");
+    p.useSwitchingFunction = f->as_int("useSwitchingFunction");
+    p.version = f->as_int("version");
+    if (const XmlNode *ps = f->child("Particles"))
+        for (auto *q : ps->children_named("Particle"))
+            p.particles.push_back(NbParticle{q->as_double("q"), q->as_double("sig"), q->as_double("eps")});
+    if (const XmlNode *es = f->child("Exceptions"))
+        for (auto *e : es->children_named("Exception"))
+            p.exceptions.push_back(NbException{e->as_int("p1"), e->as_int("p2"), e->as_double("q"), e->as_double("sig"),
+                                               e->as_double("eps")});
+    return p;
+}
+
+std::vector<double> positions_of(const XmlDoc &d) {
+    std::vector<double> out;
+    const XmlNode *st = d.root.child("State");
+    const XmlNode *ps = st ? st->child("Positions") : nullptr;
+    if (ps)
+        for (auto *q : ps->children_named("Position")) {
+            out.push_back(q->as_double("x"));
+            out.push_back(q->as_double("y"));
+            out.push_back(q->as_double("z"));
+        }
+    return out;
+}
+
+}  // namespace
+
+std::vector<double> parse_masses(const std::string &f) {
+    XmlDoc d;
+    return load(f, d) ? masses_of(d) : std::vector<double>();
+}
+std::vector<TorsionP> parse_torsions(const std::string &f) {
+    XmlDoc d;
+    return load(f, d) ? torsions_of(d) : std::vector<TorsionP>();
+}
+std::vector<BondP> parse_bonds(const std::string &f) {
+    XmlDoc d;
+    return load(f, d) ? bonds_of(d) : std::vector<BondP>();
+}
+std::vector<AngleP> parse_angles(const std::string &f) {
+    XmlDoc d;
+    return load(f, d) ? angles_of(d) : std::vector<AngleP>();
+}
+NbParams parse_nonbonded(const std::string &f) {
+    XmlDoc d;
+    return load(f, d) ? nonbonded_of(d) : NbParams();
+}
+std::vector<double> parse_state_positions(const std::string &f) {
+    XmlDoc d;
+    return load(f, d) ? positions_of(d) : std::vector<double>();
+}
+
+bool xml_ok(const std::string &path) { return xml_load_file(path).error.empty(); }
+
+ParsedSystem parse_all(const std::string &system_xml, const std::string &state_xml) {
+    ParsedSystem ps;
+    XmlDoc st;
+    if (!state_xml.empty() && load(state_xml, st)) ps.positions = positions_of(st);
+    XmlDoc d;
+    if (!system_xml.empty() && load(system_xml, d)) {
+        ps.masses = masses_of(d);
+        ps.torsions = torsions_of(d);
+        ps.bonds = bonds_of(d);
+        ps.angles = angles_of(d);
+        ps.nb = nonbonded_of(d);
+    }
+    return ps;
+}
+
+// ------------------------------------------------------------------ reports
+
+namespace {
+
+const std::set<std::string> kAminoAcids = {"ALA", "ARG", "ASN", "ASP", "CYS", "GLN", "GLU", "GLY", "HIS", "ILE",
+                                           "LEU", "LYS", "MET", "PHE", "PRO", "SER", "THR", "TRP", "TYR", "VAL"};
+
+// Reporter.cpp:98-107
+std::string element_of(const std::string &name) {
+    if (name.empty()) return "";
+    std::string e(1, name[0]);
+    if (name.size() > 1 && std::islower((unsigned char)name[1])) e += name[1];
+    return e;
+}
+
+// Reporter.cpp:109-118: whitespace-separated fields, chain fixed to 'A';
+// a field that does not read leaves the rest at zero.
+PdbAtom parse_pdb_line(const std::string &line) {
+    PdbAtom a;
+    std::istringstream ss(line);
+    ss >> a.recordType >> a.atomNum >> a.atomName >> a.resName >> a.resSeq >> a.coords[0] >> a.coords[1] >> a.coords[2] >>
+        a.occupancy >> a.tempFactor;
+    a.chainID = 'A';
+    a.element = element_of(a.atomName);
+    a.recordType = kAminoAcids.count(a.resName) ? "ATOM  " : "HETATM";
+    return a;
+}
+
+std::string date_today() {
+    std::time_t t = std::time(nullptr);
+    char buf[32];
+    std::strftime(buf, sizeof buf, "%Y-%m-%d", std::localtime(&t));
+    return buf;
+}
+
+// Reporter.cpp:145-169
+std::string pdb_line(const PdbAtom &a) {
+    char buf[256];
+    std::snprintf(buf, sizeof buf, "%-6s%5d %-4s %3s %c%4d    %8.3f%8.3f%8.3f%6.2f%6.2f          %-2s",
+                  a.recordType.c_str(), a.atomNum, a.atomName.c_str(), a.resName.c_str(), a.chainID, a.resSeq,
+                  a.coords[0], a.coords[1], a.coords[2], a.occupancy, a.tempFactor, a.element.c_str());
+    return buf;
+}
+
+}  // namespace
+
+ReportWriter::ReportWriter(const std::string &input_pdb, const std::string &output_pdb)
+    : in_(input_pdb), out_(output_pdb) {}
+
+bool ReportWriter::pdb_part1() {
+    std::ofstream out(out_);
+    std::ifstream in(in_);
+    if (!in) {
+        std::cerr << "Failed to open input file." << std::endl;
+    } else {
+        std::string line;
+        while (std::getline(in, line)) {
+            if (line.substr(0, 4) == "ATOM")
+                tmpl_.push_back(parse_pdb_line(line));
+            else if (line.substr(0, 6) == "CRYST1")
+                pbc_line_ = line;
+        }
+    }
+    out << "REMARK   Generated by Nexaus 1.0.0, " << date_today() << std::endl;
+    out << pbc_line_ << std::endl;
+    return true;
+}
+
+bool ReportWriter::pdb_part2(const double *pos, int model) {
+    std::ofstream out(out_, std::ios::out | std::ios::app);
+    if (!out.is_open()) {
+        std::cerr << "Unable to open the file: " << out_ << std::endl;
+        return false;
+    }
+    std::cout << model << "   ";
+    out << "MODEL        " << model << std::endl;
+    for (size_t i = 0; i < tmpl_.size(); ++i) {
+        PdbAtom a = tmpl_[i];
+        for (int c = 0; c < 3; ++c) a.coords[c] = pos[3 * (size_t)(a.atomNum - 1) + c] * 10.0;
+        out << pdb_line(a) << std::endl;
+        if (i == tmpl_.size() - 1) {
+            char buf[128];
+            std::snprintf(buf, sizeof buf, "%-6s%5d %-4s %3s %c%4d", "TER", tmpl_[i].atomNum + 1, "",
+                          tmpl_[i].resName.c_str(), tmpl_[i].chainID, tmpl_[i].resSeq);
+            out << buf << std::endl;
+        }
+    }
+    out << "ENDMDL" << std::endl;
+    return true;
+}
+
+bool ReportWriter::total_energy(double ke, double pe, double te, int step) {
+    std::string name = "TotalEnergy" + out_;
+    std::ofstream out(name, step == 0 ? std::ios::out : (std::ios::out | std::ios::app));
+    if (!out.is_open()) {
+        std::cerr << "Unable to open the file: " << name << std::endl;
+        return false;
+    }
+    char buf[256];
+    if (step == 0) {
+        out << "Step\tTotal Kinetic Energy (kJ/mol)\tTotal Potential Energy (kJ/mol)\tTotal Energy (kJ/mol)\n";
+        std::snprintf(buf, sizeof buf, "%5d%25.10f%30.10f%25.10f\n", step, ke, pe, te);
+    } else {
+        std::snprintf(buf, sizeof buf, "%5d%25g%30g%25g\n", step, ke, pe, te);
+    }
+    out << buf;
+    return true;
+}
+
+bool ReportWriter::pvf(const double *pos, const double *vel, const double *frc, int n, int step) {
+    std::string name = "PVFReport" + out_;
+    std::ofstream out(name, step == 0 ? std::ios::out : (std::ios::out | std::ios::app));
+    if (!out.is_open()) {
+        std::cerr << "Unable to open the file: " << name << std::endl;
+        return false;
+    }
+    out << "Step" << step << "\n";
+    out << "ID\tPosition(nm)\t\t\tVelocity(nm / ps)\t\tForce(kJ / mol * nm)\n";
+    std::string buf;
+    buf.reserve((size_t)n * 160);
+    char line[512];
+    for (int i = 0; i < n; ++i) {
+        const double *p = pos + 3 * (size_t)i, *v = vel + 3 * (size_t)i, *f = frc + 3 * (size_t)i;
+        std::snprintf(line, sizeof line,
+                      "%d\t(%10.10f, %10.10f, %10.10f)\t(%10.10f, %10.10f, %10.10f)\t(%10.10f, %10.10f, %10.10f)\n", i + 1,
+                      p[0], p[1], p[2], v[0], v[1], v[2], f[0], f[1], f[2]);
+        buf += line;
+    }
+    out << buf << "\n";
+    return true;
+}
+
+}  // namespace nxm

@@ -53,6 +53,34 @@ def main():
             E_nonbonded=np.array([En["recip"], En["self"], En["direct"], En["exclusion_signed"]]),
             F_total=Ftot, v0=v0, pos1=p1, vel1=v1, ke=ke)
         print(name, s.n, "atoms,", len(pairs), "pairs")
+    simulate_case(r)
+
+
+def simulate_case(r):
+    """The reference's own Simulate on a small system: inputs and the three
+    report files it writes (PVFReport<out>, TotalEnergy<out>, <out>)."""
+    import gzip
+    import shutil
+    import tempfile
+    d = os.path.join(HERE, "simulate_small")
+    os.makedirs(d, exist_ok=True)
+    s = sy.compat_system(sy.make_system(1, 4, 60, 2.4, seed=21))
+    sy.write_inputs(s, d, "small")
+    with tempfile.TemporaryDirectory() as tmp:
+        cwd = os.getcwd()
+        os.chdir(tmp)
+        try:
+            for i, (steps, interval) in enumerate(((10, 1), (7, 3))):
+                out = "out%d.pdb" % i
+                rc = r.simulate(os.path.join(d, "system_small.xml"), os.path.join(d, "state_small.xml"),
+                                os.path.join(d, "small.pdb"), out, 0.0005, steps, interval)
+                assert rc == 0
+                for f in (out, "PVFReport" + out, "TotalEnergy" + out):
+                    with open(f, "rb") as src, gzip.open(os.path.join(d, f + ".gz"), "wb") as dst:
+                        shutil.copyfileobj(src, dst)
+        finally:
+            os.chdir(cwd)
+    print("simulate_small", s.n, "atoms")
 
 
 if __name__ == "__main__":

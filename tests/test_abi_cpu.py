@@ -1,0 +1,87 @@
+"""The C ABI library and the host-side parsers, without a GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from nexusmd_gb300 import synthetic as sy
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for h in ("include/nxm.h",):
+        txt = open(os.path.join(ROOT, h)).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        names |= set(re.findall(r"\b(nxm_[a-z0-9_]+)\s*\(", txt))
+    return names
+
+
+def test_library_exports_every_declared_symbol():
+    from nexusmd_gb300.engine import load_library
+    L = load_library()
+    missing = [n for n in sorted(declared_symbols()) if not hasattr(L, n)]
+    assert not missing, missing
+    assert b"sm_103a" in L.nxm_version()
+
+
+def test_create_without_gpu_fails_loudly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from nexusmd_gb300.engine import Engine, NxmError
+    s = sy.make_system(1, 2, 20, 2.2, seed=1)
+    with pytest.raises(NxmError, match="no CUDA device"):
+        Engine(s)
+
+
+def test_parsers_round_trip(tmp_path):
+    import NexusMD
+    s = sy.make_system(1, 5, 30, 2.3, seed=9)
+    sp, st, pdb = sy.write_inputs(s, str(tmp_path), "t")
+    assert NexusMD.SystemXMLParser.MassesParser(sp) == list(s.mass)
+    b = NexusMD.SystemXMLParser.HBondParser(sp)
+    assert [(x.p1, x.p2, x.d, x.k) for x in b] == [(int(i), int(j), d, k) for (i, j), (d, k) in zip(s.bonds, s.bond_prm)]
+    a = NexusMD.SystemXMLParser.HAngleParser(sp)
+    assert [(x.p1, x.p2, x.p3, x.a, x.k) for x in a] == [
+        (int(i), int(j), int(k), th, kk) for (i, j, k), (th, kk) in zip(s.angles, s.angle_prm)]
+    t = NexusMD.SystemXMLParser.PTorsionParser(sp)
+    assert [(x.p1, x.p4, x.k, x.phase, x.periodicity) for x in t] == [
+        (int(q[0]), int(q[3]), p[0], p[1], int(n)) for q, p, n in zip(s.torsions, s.torsion_prm, s.torsion_n)]
+    nb = NexusMD.SystemXMLParser.NonBondedParser(sp)
+    assert nb.cutoff == s.cutoff and nb.ewaldTolerance == s.ewald_tol
+    assert [(p.q, p.sig, p.eps) for p in nb.particles] == list(zip(s.charge, s.sigma, s.epsilon))
+    pos = NexusMD.StateXMLParser.parseStateXML(st)
+    assert np.array_equal(np.array([p.data for p in pos]), s.pos)
+
+
+def test_parser_conventions(tmp_path, capfd):
+    """Missing attributes read as 0; an unreadable file prints the reference's
+    message and yields empty results (SystemXMLParser.cpp:22-25)."""
+    import NexusMD
+    p = tmp_path / "s.xml"
+    p.write_text('<?xml version="1.0"?>\n<!-- c --><System><Particles><Particle mass="1.5"/><Particle/>'
+                 '</Particles><Forces><Force type="HarmonicBondForce"><Bonds><Bond p1="0" p2="1" d="0.1"/>'
+                 '</Bonds></Force><Force type="HarmonicBondForce"><Bonds><Bond p1=\'1\' p2="2" k="5"/>'
+                 '</Bonds></Force></Forces></System>')
+    assert NexusMD.SystemXMLParser.MassesParser(str(p)) == [1.5, 0.0]
+    b = NexusMD.SystemXMLParser.HBondParser(str(p))
+    assert [(x.p1, x.p2, x.d, x.k) for x in b] == [(0, 1, 0.1, 0.0), (1, 2, 0.0, 5.0)]
+    nb = NexusMD.SystemXMLParser.NonBondedParser(str(p))
+    assert nb.particles == [] and "No NonbondedForce found in the XML." in capfd.readouterr().err
+    bad = tmp_path / "bad.xml"
+    bad.write_text("<System><Particles></System>")
+    assert NexusMD.SystemXMLParser.MassesParser(str(bad)) == []
+    assert "parsed with errors" in capfd.readouterr().err
+    assert NexusMD.SystemXMLParser.MassesParser(str(tmp_path / "missing.xml")) == []
+
+
+def test_dispatcher_factory_messages(capfd):
+    import NexusMD
+    NexusMD.TaskDispatcher.CreateDispatcher("GPU")
+    assert capfd.readouterr().err == ""
+    NexusMD.TaskDispatcher.CreateDispatcher("CPU")
+    assert "Invalid processor type" in capfd.readouterr().err

@@ -1,0 +1,81 @@
+"""TaskDispatcher.Simulate through the C ABI vs the reference's own Simulate.
+
+tests/golden/simulate_small holds the inputs and the three report files the
+reference wrote for them (made by tests/golden/make_golden.py).  The FP64
+engine must reproduce every line: formats byte-for-byte (headers, widths,
+record layout, model numbering), numbers to round-off.
+"""
+import gzip
+import os
+import re
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "simulate_small")
+NUM = re.compile(r"-?\d+\.\d+(?:e[+-]\d+)?|-?\d+(?:e[+-]\d+)?")
+
+
+def _gold(name):
+    with gzip.open(os.path.join(GOLD, name + ".gz"), "rt") as f:
+        return f.read().splitlines()
+
+
+def _lines_match(got, ref, rtol, atol):
+    """Same text, or the same text with numbers equal within tolerance."""
+    if got == ref:
+        return True
+    if NUM.sub("#", got) != NUM.sub("#", ref):
+        return False
+    a = [float(x) for x in NUM.findall(got)]
+    b = [float(x) for x in NUM.findall(ref)]
+    return len(a) == len(b) and np.allclose(a, b, rtol=rtol, atol=atol)
+
+
+def _run(tmp_path, precision, steps, interval, idx):
+    import NexusMD
+    d = NexusMD.TaskDispatcher.CreateDispatcher("GPU")
+    d.EnableHarmonicBondForce()
+    d.EnableHarmonicAngleForce()
+    d.EnablePeriodicTorsionForce()
+    d.EnableNonbondedForce()
+    d.SetOptions(precision=precision, skin=0.1, rebuild_interval=10)
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        out = "out%d.pdb" % idx
+        d.Simulate(os.path.join(GOLD, "system_small.xml"), os.path.join(GOLD, "state_small.xml"),
+                   os.path.join(GOLD, "small.pdb"), out, 0.0005, steps, interval)
+        return {f: open(os.path.join(tmp_path, f)).read().splitlines()
+                for f in (out, "PVFReport" + out, "TotalEnergy" + out)}
+    finally:
+        os.chdir(cwd)
+
+
+@pytest.mark.parametrize("steps,interval,idx", [(10, 1, 0), (7, 3, 1)])
+def test_simulate_fp64_matches_reference_files(tmp_path, steps, interval, idx):
+    got = _run(tmp_path, "fp64", steps, interval, idx)
+    for name, lines in got.items():
+        ref = _gold(name)
+        assert len(lines) == len(ref), name
+        for k, (a, b) in enumerate(zip(lines, ref)):
+            if a.startswith("REMARK   Generated by"):
+                assert b.startswith("REMARK   Generated by")
+                continue
+            # positions/velocities to 1e-9, forces and energies to 1e-8 relative
+            assert _lines_match(a, b, rtol=1e-8, atol=2e-9), (name, k, a, b)
+
+
+def test_simulate_mixed_precision_tracks_reference(tmp_path):
+    got = _run(tmp_path, "mixed", 10, 1, 0)
+    ref = _gold("TotalEnergyout0.pdb")
+    te = got["TotalEnergyout0.pdb"]
+    assert te[0] == ref[0] and len(te) == len(ref)
+    a = np.array([[float(x) for x in l.split()] for l in te[1:]])
+    b = np.array([[float(x) for x in l.split()] for l in ref[1:]])
+    assert np.allclose(a[:, 1:], b[:, 1:], rtol=2e-4, atol=0.05)
+    pvf, rpvf = got["PVFReportout0.pdb"], _gold("PVFReportout0.pdb")
+    assert len(pvf) == len(rpvf)
+    assert all(NUM.sub("#", x) == NUM.sub("#", y) for x, y in zip(pvf, rpvf))
