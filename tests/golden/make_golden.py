@@ -64,7 +64,7 @@ def simulate_case(r):
     import tempfile
     d = os.path.join(HERE, "simulate_small")
     os.makedirs(d, exist_ok=True)
-    s = sy.compat_system(sy.make_system(1, 4, 60, 2.4, seed=21))
+    s = sy.compat_system(sy.make_system(1, 4, 100, 2.8, seed=21))
     sy.write_inputs(s, d, "small")
     with tempfile.TemporaryDirectory() as tmp:
         cwd = os.getcwd()
