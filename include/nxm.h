@@ -185,6 +185,32 @@ int nxm_dispatcher_simulate(nxm_dispatcher *d, const char *system_xml, const cha
                             const char *input_pdb, const char *output_pdb, double step_size,
                             int32_t total_steps, int32_t interval);
 
+/* ---- Reciprocal-space PME that allocates nothing.  No counterpart in the
+ * reference (its PME allocates its grids on every evaluation).
+ *
+ * The engine's mixed-precision PME step (order-5 B-splines, int64
+ * fixed-point charge grid, FP32 FFT, influence function and energy) for one
+ * system, on caller-owned DEVICE buffers, enqueued on `stream` (a
+ * cudaStream_t; NULL = the legacy default stream) and not waited for:
+ *   xyz      n_atoms x 3 doubles, nm (read)
+ *   charge   n_atoms doubles, e (read)
+ *   force    n_atoms x 3 doubles, kJ/mol/nm (overwritten: reciprocal force)
+ *   energy   1 double, kJ/mol (overwritten: reciprocal energy)
+ * Host arguments: box corners (box edge = |ub - lb|; the grid is anchored at
+ * the origin as in the reference), grid sizes, Ewald alpha (1/nm).
+ * All intermediates live in one static device array of about 4.8 MB per
+ * device, so each grid axis must be 2^a 3^b 5^c with 5 <= K <= 64; a larger
+ * grid returns NXM_ERR_CAPACITY.  It calls no cudaMalloc, cudaFree or other
+ * allocating routine and copies nothing between host and device.
+ * The first call on a device (the current one) looks up the array's address
+ * (cudaGetSymbolAddress, which may load the module): make it before any
+ * stream capture.  Every call on a device shares the array and finds the
+ * previous call's contents; each call clears what must start at zero, but
+ * calls whose work overlaps on the GPU race: serialise them. */
+int nxm_pme_reciprocal_noalloc(const double *xyz, const double *charge, int32_t n_atoms,
+                               const double box_lb[3], const double box_ub[3], const int32_t grid[3],
+                               double alpha, double *force, double *energy, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
