@@ -148,6 +148,12 @@ int nxm_time_steps(nxm_ctx *ctx, int32_t nsteps, double dt, double *ms);
  * [6] PME gather, [7] integrate.  cap >= 8. */
 int nxm_profile_phases(nxm_ctx *ctx, int32_t nsteps, double dt, double *ms, int32_t cap);
 
+/* Neighbour-list rebuilds since nxm_create (waits for the context's work).
+ * The reference rebuilds on every force evaluation (NeighborList.cpp:129-154
+ * via NonbondedForce.cpp:474-500); this engine rebuilds when the device
+ * decides (list age or displacement beyond half the skin). */
+int nxm_rebuild_count(nxm_ctx *ctx, int64_t *count);
+
 /* Kernel launches one step issues (steady state, no list rebuild). */
 int nxm_launches_per_step(nxm_ctx *ctx, int32_t *launches, int32_t *rebuild_launches);
 

@@ -210,6 +210,14 @@ int nxm_profile_phases(nxm_ctx *ctx, int32_t nsteps, double dt, double *ms, int3
     NXM_CALL(ctx->eng.profile(nsteps, dt, ms));
 }
 
+int nxm_rebuild_count(nxm_ctx *ctx, int64_t *count) {
+    if (!ctx || !count) return fail(NXM_ERR_INVALID, "null argument");
+    std::string e = ctx->eng.sync();
+    if (!e.empty()) return fail(code_for(e), e);
+    *count = ctx->eng.rebuild_count();
+    return NXM_OK;
+}
+
 int nxm_launches_per_step(nxm_ctx *ctx, int32_t *launches, int32_t *rebuild_launches) {
     if (!ctx) return fail(NXM_ERR_INVALID, "null argument");
     if (launches) *launches = ctx->eng.launches_per_step();

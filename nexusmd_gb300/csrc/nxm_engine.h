@@ -71,6 +71,8 @@ public:
     const SysHost &sys(int s) const { return sysh_[s]; }
     int launches_per_step() const { return launches_per_step_; }
     int launches_per_rebuild() const { return launches_per_rebuild_; }
+    // neighbour-list rebuilds since creation, as of the last finished call
+    long long rebuild_count() const { return h_flags_ ? reinterpret_cast<const Flags *>(h_flags_)->nrebuild : 0; }
 
 private:
     std::string one_step(double dt, int report);

@@ -86,6 +86,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.nxm_time_steps.argtypes = [C.c_void_p, C.c_int32, C.c_double, C.POINTER(C.c_double)]
     L.nxm_profile_phases.argtypes = [C.c_void_p, C.c_int32, C.c_double, dp, C.c_int32]
     L.nxm_launches_per_step.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    L.nxm_rebuild_count.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
     L.nxm_n_atoms.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
     _lib = L
     return L
@@ -256,3 +257,9 @@ class Engine:
         a, b = C.c_int32(), C.c_int32()
         _check(self._L.nxm_launches_per_step(self._h, C.byref(a), C.byref(b)), "launches")
         return a.value, b.value
+
+    def rebuilds(self):
+        """Neighbour-list rebuilds since the context was created."""
+        n = C.c_int64()
+        _check(self._L.nxm_rebuild_count(self._h, C.byref(n)), "rebuild_count")
+        return n.value
