@@ -275,7 +275,8 @@ def native(args):
                                           % (s.n * 560 * 2 / 1e6)},
            "e2e": {"value": ws * s.n * args.steps / e2e_s, "unit": "atom-steps/s",
                    "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h},
-           "gpu_launches": launches * args.steps,
+           # per step: the step's kernels (one graph launch); per list rebuild: the rebuild kernels
+           "gpu_launches": launches * args.steps + rb_launches * rebuilds,
            "clocks": clk.summary()}
     out["ns_per_day"] = (1.0 / (per_step * 1e-3)) * DT_PS * 1e-3 * 86400.0
 

@@ -86,7 +86,7 @@ __device__ int stage(const DevView &v, const SysDev &S, int sys, int c3_first, i
             }
             if (MIXED && !BUILD) s_lj[k] = v.ljf[j];
             if (BUILD) {
-                s_slot[k] = j;
+                if (s_slot) s_slot[k] = j;
                 s_orig[k] = v.orig[j];
             }
         }
@@ -102,9 +102,52 @@ __device__ __forceinline__ int list_pos(int p) { return (p & ~255) | ((p & 31) <
 
 // ------------------------------------------------------------------ build
 
+constexpr int kRowCells = kMaxGroup + 4;  // cells of one neighbourhood row, at most
+
+// Tile index of the first atom of every cell of every neighbourhood row
+// (bnd[r * (kRowCells + 1) + oz + 2], oz = -2 .. g + 1) and of the row's end
+// (index g + 4): the same enumeration as hood_spans, so cell ranges of the
+// tile are contiguous index ranges.
+__device__ __forceinline__ void hood_cell_bounds(const DevView &v, const SysDev &S, int c3, int g, int *bnd) {
+    if (threadIdx.x < 32) {
+        int lane = threadIdx.x;
+        int ncz = S.nc[2], cz0 = (c3 >> 20) & 1023;
+        int rowkey = 0, tot = 0;
+        if (lane < 25) {
+            int nx = hood_wrap((c3 & 1023) + lane / 5 - 2, S.nc[0]);
+            int ny = hood_wrap(((c3 >> 10) & 1023) + lane % 5 - 2, S.nc[1]);
+            rowkey = S.cell_off + (nx * S.nc[1] + ny) * ncz;
+            for (int oz = -2; oz <= g + 1; ++oz) {
+                int cz = hood_wrap(cz0 + oz, ncz);
+                tot += v.cell_start[rowkey + cz + 1] - v.cell_start[rowkey + cz];
+            }
+        }
+        int off = tot;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int a = __shfl_up_sync(0xffffffffu, off, o);
+            if (lane >= o) off += a;
+        }
+        off -= tot;
+        if (lane < 25) {
+            int *b = bnd + lane * (kRowCells + 1);
+            for (int oz = -2; oz <= g + 1; ++oz) {
+                int cz = hood_wrap(cz0 + oz, ncz);
+                b[oz + 2] = off;
+                off += v.cell_start[rowkey + cz + 1] - v.cell_start[rowkey + cz];
+            }
+            b[g + 4] = off;
+        }
+    }
+    __syncthreads();
+}
+
 // Each warp takes atoms of the group; every staged atom within the list
 // radius that is not i itself and not excluded is appended to i's list as
-// its 16-bit tile index (ballot compaction: deterministic order).
+// its 16-bit tile index (ballot compaction: deterministic order).  An atom
+// scans only the rows of the neighbourhood its list sphere reaches, and in
+// each row only the z-cells it reaches (with a 0.01 nm margin over the cell
+// bounds), in tile order: the list is the one a scan of the whole tile gives.
 __global__ void __launch_bounds__(kHoodWarps * 32) k_build(DevView v) {
     extern __shared__ __align__(16) unsigned char smem[];
     if (!v.flags->rebuild) return;
@@ -119,20 +162,32 @@ __global__ void __launch_bounds__(kHoodWarps * 32) k_build(DevView v) {
     }
     int cap = v.hood_cap;
     float4 *s_q = reinterpret_cast<float4 *>(smem);
-    int *s_slot = reinterpret_cast<int *>(s_q + cap);
-    int *s_orig = s_slot + cap;
-    HoodSpan *spans = reinterpret_cast<HoodSpan *>(s_orig + cap);
+    int *s_orig = reinterpret_cast<int *>(s_q + cap);
+    int *s_bnd = s_orig + cap;
+    HoodSpan *spans = reinterpret_cast<HoodSpan *>(s_bnd + 25 * (kRowCells + 1));
     int *s_n = reinterpret_cast<int *>(spans + kMaxSpans);
     int c3f = v.cell3[a0];
-    int n = v.mixed ? stage<true, true>(v, S, G.sys, c3f, G.ncell, s_q, nullptr, s_slot, s_orig, spans, s_n)
-                    : stage<true, false>(v, S, G.sys, c3f, G.ncell, s_q, nullptr, s_slot, s_orig, spans, s_n);
+    int n = v.mixed ? stage<true, true>(v, S, G.sys, c3f, G.ncell, s_q, nullptr, nullptr, s_orig, spans, s_n)
+                    : stage<true, false>(v, S, G.sys, c3f, G.ncell, s_q, nullptr, nullptr, s_orig, spans, s_n);
     if (n < 0) return;
+    hood_cell_bounds(v, S, c3f, G.ncell, s_bnd);
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     float rl2 = S.rlist2f * 1.0001f + 1e-6f;
+    const float margin = 0.01f;
+    const float rlm = sqrtf(rl2) + margin;
+    const float csx = (float)S.cs[0], csy = (float)S.cs[1], csz = (float)S.cs[2], icsz = 1.0f / csz;
     int czf = (c3f >> 20) & 1023;
+    int g = G.ncell;
     for (int i = a0 + warp; i < a1; i += nw) {
         float pi3[3];
         i_in_group_frame(v, S, i, czf, pi3);
+        // i's own tile index: row (0, 0), cell oz_i counted from the
+        // neighbourhood's anchor cell (the group's first non-empty cell)
+        int c3i = v.cell3[i];
+        int cz_i = (c3i >> 20) & 1023;
+        int oz_i = hood_wrap(cz_i - czf, S.nc[2]);
+        int key_i = S.cell_off + ((c3i & 1023) * S.nc[1] + ((c3i >> 10) & 1023)) * S.nc[2] + cz_i;
+        int ki = s_bnd[12 * (kRowCells + 1) + oz_i + 2] + (i - v.cell_start[key_i]);
         int oi = v.orig[i];
         int e0 = v.excl_off[oi];
         int ne = v.excl_off[oi + 1] - e0;
@@ -143,29 +198,43 @@ __global__ void __launch_bounds__(kHoodWarps * 32) k_build(DevView v) {
         int ex_lo = ne ? v.excl_lst[e0] : 1, ex_hi = ne ? v.excl_lst[e0 + ne - 1] : 0;
         int count = 0;
         uint16_t *out = v.nl16 + (size_t)i * v.stride;
-        for (int k0 = 0; k0 < n; k0 += 32) {
-            int k = k0 + lane;
-            bool cand = false;
-            if (k < n) {
-                float4 q = s_q[k];
-                float dx = pi3[0] - q.x, dy = pi3[1] - q.y, dz = pi3[2] - q.z;
-                cand = dx * dx + dy * dy + dz * dz < rl2 && s_slot[k] != i;
+        for (int r = 0; r < 25; ++r) {
+            // distance from i to the row's cell column in x and y
+            float ox = (float)(r / 5 - 2), oy = (float)(r % 5 - 2);
+            float ddx = fmaxf(fmaxf(ox * csx - pi3[0], pi3[0] - (ox + 1.0f) * csx), 0.0f);
+            float ddy = fmaxf(fmaxf(oy * csy - pi3[1], pi3[1] - (oy + 1.0f) * csy), 0.0f);
+            float rem = rlm * rlm - (ddx * ddx + ddy * ddy);
+            if (rem < 0.0f) continue;
+            float h = sqrtf(rem) + margin;
+            int zlo = max((int)floorf((pi3[2] - h) * icsz), -2);
+            int zhi = min((int)floorf((pi3[2] + h) * icsz), g + 1);
+            if (zlo > zhi) continue;
+            const int *b = s_bnd + r * (kRowCells + 1);
+            int kb = b[zlo + 2], ke = b[zhi + 3];
+            for (int k0 = kb; k0 < ke; k0 += 32) {
+                int k = k0 + lane;
+                bool cand = false;
+                if (k < ke) {
+                    float4 q = s_q[k];
+                    float dx = pi3[0] - q.x, dy = pi3[1] - q.y, dz = pi3[2] - q.z;
+                    cand = dx * dx + dy * dy + dz * dz < rl2 && k != ki;
+                }
+                if (!__any_sync(full, cand)) continue;
+                int oj = cand ? s_orig[k] : -2;
+                bool ex = false;
+                if (__any_sync(full, cand && oj >= ex_lo && oj <= ex_hi)) {
+                    for (int e = 0; e < nfast; ++e) ex |= (__shfl_sync(full, my_ex, e) == oj);
+                    if (ne > 32 && cand)
+                        for (int e = 32; e < ne; ++e) ex |= (v.excl_lst[e0 + e] == oj);
+                }
+                bool ok = cand && !ex;
+                unsigned m = __ballot_sync(full, ok);
+                if (ok) {
+                    int pos = count + __popc(m & ((1u << lane) - 1u));
+                    if (pos < v.stride) out[list_pos(pos)] = (uint16_t)k;
+                }
+                count += __popc(m);
             }
-            if (!__any_sync(full, cand)) continue;
-            int oj = cand ? s_orig[k] : -2;
-            bool ex = false;
-            if (__any_sync(full, cand && oj >= ex_lo && oj <= ex_hi)) {
-                for (int e = 0; e < nfast; ++e) ex |= (__shfl_sync(full, my_ex, e) == oj);
-                if (ne > 32 && cand)
-                    for (int e = 32; e < ne; ++e) ex |= (v.excl_lst[e0 + e] == oj);
-            }
-            bool ok = cand && !ex;
-            unsigned m = __ballot_sync(full, ok);
-            if (ok) {
-                int pos = count + __popc(m & ((1u << lane) - 1u));
-                if (pos < v.stride) out[list_pos(pos)] = (uint16_t)k;
-            }
-            count += __popc(m);
         }
         if (lane == 0) {
             v.ncount[i] = count < v.stride ? count : v.stride;
@@ -181,13 +250,16 @@ struct PairPrm {
     int use_sw;
 };
 
-// FP32 force (and energy) of one pair inside the cutoff, accumulated into
-// the lane's partial sums (NonbondedForce.cpp:559-581 in single precision).
-template <bool ENERGY>
-__device__ __forceinline__ void pair_mixed(float dx, float dy, float dz, float r2, float qq, float sg, float eps,
-                                           const PairPrm &P, float &fx, float &fy, float &fz, float &ec,
-                                           float &ev) {
-    float rinv = rsqrtf(r2);
+// FP32 force (and energy) of one list entry, accumulated into the lane's
+// partial sums when `in` (inside the cutoff), NonbondedForce.cpp:559-581 in
+// single precision.  Evaluated without branches: an entry outside the cutoff
+// (r^2 up to 1e30 for padding) gives finite values that the select drops, so
+// two entries per lane run as independent instruction streams.
+template <bool ENERGY, bool SW>
+__device__ __forceinline__ void pair_mixed(bool in, float dx, float dy, float dz, float r2, float qq, float sg,
+                                           float eps, const PairPrm &P, float &fx, float &fy, float &fz,
+                                           float &ec, float &ev) {
+    float rinv = fast_rsqrt(r2);
     float rinv2 = rinv * rinv;
     float r = r2 * rinv;
     float xa = P.alpha * r;
@@ -198,26 +270,29 @@ __device__ __forceinline__ void pair_mixed(float dx, float dy, float dz, float r
     float s6 = s2 * s2 * s2;
     float evdw = eps * (s6 - 1.0f) * s6;
     float sw = 1.0f;
-    if (P.use_sw && r > P.sw) {
+    if (SW && P.use_sw && r > P.sw) {
         float w = P.cut - P.sw;
         float t = (r - P.sw) / w;
         sw = 1.0f + t * t * t * (-10.0f + t * (15.0f - t * 6.0f));
         float dsw = t * t * (-30.0f + t * (60.0f - t * 30.0f)) / w;
         dEdR -= evdw * dsw * rinv;
     }
-    dEdR = fmaf(sw * eps * (12.0f * s6 - 6.0f) * s6, rinv2, dEdR);
+    float lj = eps * (12.0f * s6 - 6.0f) * s6;
+    if (SW) lj *= sw;
+    dEdR = fmaf(lj, rinv2, dEdR);
+    dEdR = in ? dEdR : 0.0f;
     fx = fmaf(dx, dEdR, fx);
     fy = fmaf(dy, dEdR, fy);
     fz = fmaf(dz, dEdR, fz);
     if (ENERGY) {
-        ec = fmaf(qq * rinv, erfcv, ec);
-        ev = fmaf(sw, evdw, ev);
+        ec += in ? qq * rinv * erfcv : 0.0f;
+        ev += in ? (SW ? sw * evdw : evdw) : 0.0f;
     }
 }
 
 // Mixed precision: each lane keeps two list entries in flight; j comes from
-// the staged tile.
-template <bool ENERGY>
+// the staged tile.  SW: some system of the batch uses the switching function.
+template <bool ENERGY, bool SW>
 __global__ void __launch_bounds__(kHoodWarps * 32) k_pairs_mixed(DevView v) {
     extern __shared__ __align__(16) unsigned char smem[];
     const unsigned full = 0xffffffffu;
@@ -255,6 +330,7 @@ __global__ void __launch_bounds__(kHoodWarps * 32) k_pairs_mixed(DevView v) {
             uint32_t wds[4] = {cur.x, cur.y, cur.z, cur.w};
 #pragma unroll
             for (int u = 0; u < 8; u += 2) {
+            if (c0 + 32 * u >= cnt) break;  // rest of the last chunk is empty (warp-uniform)
             int k0 = c0 + lane + 32 * u, k1 = k0 + 32;
             bool v0 = k0 < cnt, v1 = k1 < cnt;
             int t0 = v0 ? (int)(wds[u >> 1] & 0xffffu) : 0;
@@ -272,8 +348,10 @@ __global__ void __launch_bounds__(kHoodWarps * 32) k_pairs_mixed(DevView v) {
                 if (b0) in0 = exact_r2(v, S, i, hood_slot(spans, nsp, t0)) < S.cut2;
                 if (b1) in1 = exact_r2(v, S, i, hood_slot(spans, nsp, t1)) < S.cut2;
             }
-            if (in0) pair_mixed<ENERGY>(dx0, dy0, dz0, r20, qi * p0.w, li.x + l0.x, li.y * l0.y, P, fx, fy, fz, ec, ev);
-            if (in1) pair_mixed<ENERGY>(dx1, dy1, dz1, r21, qi * p1.w, li.x + l1.x, li.y * l1.y, P, fx, fy, fz, ec, ev);
+            pair_mixed<ENERGY, SW>(in0, dx0, dy0, dz0, r20, qi * p0.w, li.x + l0.x, li.y * l0.y, P, fx, fy, fz, ec,
+                                   ev);
+            pair_mixed<ENERGY, SW>(in1, dx1, dy1, dz1, r21, qi * p1.w, li.x + l1.x, li.y * l1.y, P, fx, fy, fz, ec,
+                                   ev);
             }
             cur = nxt;
         }
@@ -410,7 +488,9 @@ __global__ void k_collect(DevView v, int sys_sel, int *out, long long cap, unsig
 // ------------------------------------------------------------------ launch
 
 static size_t tail_bytes() { return kMaxSpans * sizeof(HoodSpan) + 4 * sizeof(int); }
-static size_t smem_build(int cap) { return (size_t)cap * (sizeof(float4) + 2 * sizeof(int)) + tail_bytes(); }
+static size_t smem_build(int cap) {
+    return (size_t)cap * (sizeof(float4) + sizeof(int)) + 25 * (kRowCells + 1) * sizeof(int) + tail_bytes();
+}
 static size_t smem_pairs(int cap, int mixed) {
     return mixed ? (size_t)cap * (sizeof(float4) + sizeof(float2)) + tail_bytes() : tail_bytes();
 }
@@ -418,8 +498,10 @@ static size_t smem_pairs(int cap, int mixed) {
 void tiles_set_smem(int cap) {
     int b = (int)smem_build(cap), m = (int)smem_pairs(cap, 1);
     cudaFuncSetAttribute(k_build, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    cudaFuncSetAttribute(k_pairs_mixed<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-    cudaFuncSetAttribute(k_pairs_mixed<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_pairs_mixed<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_pairs_mixed<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_pairs_mixed<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_pairs_mixed<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
 }
 
 void launch_build(const DevView &v, cudaStream_t st) {
@@ -431,10 +513,17 @@ void launch_pairs(const DevView &v, int energy, cudaStream_t st) {
     int g = v.ngroups, t = kHoodWarps * 32;
     size_t sm = smem_pairs(v.hood_cap, v.mixed);
     if (v.mixed) {
-        if (energy)
-            k_pairs_mixed<true><<<g, t, sm, st>>>(v);
-        else
-            k_pairs_mixed<false><<<g, t, sm, st>>>(v);
+        if (v.any_switch) {
+            if (energy)
+                k_pairs_mixed<true, true><<<g, t, sm, st>>>(v);
+            else
+                k_pairs_mixed<false, true><<<g, t, sm, st>>>(v);
+        } else {
+            if (energy)
+                k_pairs_mixed<true, false><<<g, t, sm, st>>>(v);
+            else
+                k_pairs_mixed<false, false><<<g, t, sm, st>>>(v);
+        }
     } else {
         if (energy)
             k_pairs_fp64<true><<<g, t, sm, st>>>(v);

@@ -30,6 +30,18 @@ __global__ void k_decide(DevView v, int force) {
 
 void launch_decide_rebuild(const DevView &v, int force, cudaStream_t st) { k_decide<<<1, 1, 0, st>>>(v, force); }
 
+// The same decision inside a step graph: it also opens or closes the
+// graph's conditional rebuild node.
+__global__ void k_decide_graph(DevView v, cudaGraphConditionalHandle h) {
+    Flags *f = v.flags;
+    int rb = f->since >= f->interval || f->skin_hit;
+    f->rebuild = rb;
+    f->skin_hit = 0;
+    f->since = rb ? 1 : f->since + 1;
+    if (rb) f->nrebuild += 1;
+    cudaGraphSetConditional(h, rb ? 1u : 0u);
+}
+
 // ------------------------------------------------------------ host maths
 
 static bool smooth235(int n) {
@@ -148,6 +160,7 @@ T *Engine::dalloc(size_t n) {
 
 Engine::~Engine() {
     if (st_) cudaStreamSynchronize(st_);
+    free_graphs();
     for (void *p : allocs_) cudaFree(p);
     fft_plan_free(plan_);
     if (h_E_) cudaFreeHost(h_E_);
@@ -620,6 +633,8 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     v_.skin_half2 = skin > 0 ? 0.25 * skin * skin : 0.0;
     v_.force_mask = 0;
     for (auto &h : sysh_) v_.force_mask |= h.force_mask;
+    v_.any_switch = 0;
+    for (auto &d : sysd_) v_.any_switch |= d.use_switch ? 1 : 0;
     cudaMallocHost(&h_E_, sizeof(long long) * S * E_SLOTS);
     cudaMallocHost(&h_flags_, sizeof(Flags));
     energies_.assign((size_t)S * E_SLOTS, 0.0);
@@ -672,6 +687,13 @@ std::string Engine::set_velocities(const double *xyz) {
 }
 
 // Force kernels of one evaluation (everything but the integrator).
+// Kernel launches of force_launches below, without launching.
+static int force_launch_count(const DevView &v) {
+    int n = (v.nb + v.na + v.nt) ? 1 : 0;
+    if (v.force_mask & NXM_FORCE_NONBONDED) n += 1 + (v.nex ? 1 : 0) + 7;
+    return n;
+}
+
 static int force_launches(const DevView &v, const FftPlan &plan, int energy, cudaStream_t st) {
     int n = 0;
     if (v.nb + v.na + v.nt) {
@@ -691,15 +713,97 @@ static int force_launches(const DevView &v, const FftPlan &plan, int energy, cud
     return n;
 }
 
-std::string Engine::one_step(double dt, int report) {
+void Engine::free_graphs() {
+    for (auto &G : graph_) {
+        if (G.exec) cudaGraphExecDestroy(G.exec);
+        if (G.graph) cudaGraphDestroy(G.graph);
+        G = StepGraph{};
+    }
+}
+
+std::string Engine::build_graph(double dt, int report) {
+    StepGraph &G = graph_[report ? 1 : 0];
+    if (G.exec) cudaGraphExecDestroy(G.exec);
+    if (G.graph) cudaGraphDestroy(G.graph);
+    G = StepGraph{};
+    const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+    cudaGraph_t g = nullptr, captured = nullptr;
+    auto fail_capture = [&](const char *what, cudaError_t e) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st_, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone)
+            cudaStreamEndCapture(st_, &captured);
+        cudaGetLastError();
+        return std::string("step graph: ") + what + ": " + cudaGetErrorString(e);
+    };
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    if (e != cudaSuccess) return fail_capture("create", e);
+    G.graph = g;
+    cudaGraphConditionalHandle h;
+    e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return fail_capture("conditional handle", e);
+    // head: energy reset and the decision
+    e = cudaStreamBeginCaptureToGraph(st_, g, nullptr, nullptr, 0, mode);
+    if (e != cudaSuccess) return fail_capture("capture head", e);
     if (report) cudaMemsetAsync(v_.E, 0, sizeof(long long) * v_.S * E_SLOTS, st_);
-    launch_decide_rebuild(v_, force_rebuild_ ? 1 : 0, st_);
+    k_decide_graph<<<1, 1, 0, st_>>>(v_, h);
+    cudaStreamCaptureStatus cs;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    e = cudaStreamGetCaptureInfo(st_, &cs, nullptr, nullptr, &deps, nullptr, &nd);
+    if (e != cudaSuccess) return fail_capture("capture info", e);
+    std::vector<cudaGraphNode_t> head(deps, deps + nd);
+    e = cudaStreamEndCapture(st_, &captured);
+    if (e != cudaSuccess) return fail_capture("end head", e);
+    // the conditional rebuild node and its body
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeIf;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cnode;
+    e = cudaGraphAddNode(&cnode, g, head.data(), nullptr, head.size(), &cp);
+    if (e != cudaSuccess) return fail_capture("conditional node", e);
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(st_, body, nullptr, nullptr, 0, mode);
+    if (e != cudaSuccess) return fail_capture("capture rebuild", e);
+    launch_nlist_rebuild(v_, st_);
+    e = cudaStreamEndCapture(st_, &captured);
+    if (e != cudaSuccess) return fail_capture("end rebuild", e);
+    // tail: forces and update, after the conditional node
+    e = cudaStreamBeginCaptureToGraph(st_, g, &cnode, nullptr, 1, mode);
+    if (e != cudaSuccess) return fail_capture("capture tail", e);
+    force_launches(v_, plan_, report, st_);
+    launch_integrate(v_, dt, report, st_);
+    e = cudaStreamEndCapture(st_, &captured);
+    if (e != cudaSuccess) return fail_capture("end tail", e);
+    e = cudaGraphInstantiate(&G.exec, g, 0);
+    if (e != cudaSuccess) return fail_capture("instantiate", e);
+    G.dt = dt;
+    G.ok = true;
+    return "";
+}
+
+std::string Engine::one_step(double dt, int report) {
+    launches_per_rebuild_ = 10;  // kernels of one list rebuild
+    if (!force_rebuild_) {
+        StepGraph &G = graph_[report ? 1 : 0];
+        if (!G.ok || G.dt != dt) {
+            std::string e = build_graph(dt, report);
+            if (!e.empty()) return e;
+        }
+        cudaError_t e = cudaGraphLaunch(G.exec, st_);
+        if (e != cudaSuccess) return std::string("step graph launch: ") + cudaGetErrorString(e);
+        // decide + forces + integrate; the rebuild kernels run on rebuild steps only
+        launches_per_step_ = force_launch_count(v_) + 2;
+        return check("step");
+    }
+    if (report) cudaMemsetAsync(v_.E, 0, sizeof(long long) * v_.S * E_SLOTS, st_);
+    launch_decide_rebuild(v_, 1, st_);
     force_rebuild_ = false;
     launch_nlist_rebuild(v_, st_);
     int n = force_launches(v_, plan_, report, st_);
     launch_integrate(v_, dt, report, st_);
-    launches_per_rebuild_ = 10;        // gated rebuild kernels, launched every step
-    launches_per_step_ = n + 2 + launches_per_rebuild_;  // decide + rebuild + forces + integrate
+    launches_per_step_ = n + 2 + launches_per_rebuild_;
     return check("step");
 }
 

@@ -75,6 +75,19 @@ public:
     long long rebuild_count() const { return h_flags_ ? reinterpret_cast<const Flags *>(h_flags_)->nrebuild : 0; }
 
 private:
+    // One step as a CUDA graph: energy reset (report steps), the list
+    // decision, a conditional node whose body is the rebuild sequence (run
+    // only when the decision kernel sets it), the force kernels and the
+    // update.  One graph per report flag, rebuilt when dt changes.
+    struct StepGraph {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        double dt = 0.0;
+        bool ok = false;
+    };
+    StepGraph graph_[2];
+    std::string build_graph(double dt, int report);
+    void free_graphs();
     std::string one_step(double dt, int report);
     std::string check(const char *what);
     std::string finish_call();

@@ -19,6 +19,7 @@ struct DevView {
     int N, S;            // atoms (slots) and systems in the batch
     int mixed;           // 1: FP32 force math + int64 fixed point; 0: FP64 throughout
     int force_mask;      // 1 bond, 2 angle, 4 torsion, 8 nonbonded
+    int any_switch;      // some system of the batch uses the LJ switching function
     const SysDev *sys;
     int *sys_of;         // slot -> system
     int *orig;           // slot -> original atom index (batch-global)

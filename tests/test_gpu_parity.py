@@ -152,3 +152,50 @@ def test_explicit_box_skin_list(oracle):
         eng = _engine(s, precision=prec, skin=0.1, rebuild_interval=10, box="explicit")
         F = eng.compute_forces()
         assert rel_rms(F, F0) <= tol, (prec, rel_rms(F, F0))
+
+
+def _sparse_gas(seed=8, n_mol=150, box=5.0):
+    """Diatomic molecules scattered in a large box: most cells are empty, so
+    many cell groups start with an empty cell (the tile is then anchored at
+    the group's first non-empty cell)."""
+    import types
+    rng = np.random.default_rng(seed)
+    pos = []
+    while len(pos) < 2 * n_mol:
+        a = rng.uniform(0, box, 3)
+        d = rng.normal(size=3)
+        b = a + 0.12 * d / np.linalg.norm(d)
+        ok = True
+        for p in pos:
+            for c in (a, b):
+                r = c - p
+                r -= box * np.round(r / box)
+                if (r * r).sum() < 0.3 ** 2:
+                    ok = False
+        if ok:
+            pos += [a, np.mod(b, box)]
+    n = len(pos)
+    q = rng.uniform(-0.8, 0.8, n)
+    bonds = np.arange(n, dtype=np.int32).reshape(-1, 2)
+    return types.SimpleNamespace(
+        n=n, pos=np.array(pos), mass=np.full(n, 12.0), charge=q, sigma=rng.uniform(0.2, 0.3, n),
+        epsilon=rng.uniform(0.1, 0.5, n), bonds=bonds, bond_prm=np.tile([0.12, 3.0e5], (n // 2, 1)),
+        angles=np.zeros((0, 3), np.int32), angle_prm=np.zeros((0, 2)), torsions=np.zeros((0, 4), np.int32),
+        torsion_prm=np.zeros((0, 2)), torsion_n=np.zeros(0, np.int32), cutoff=0.9, ewald_tol=5e-4,
+        box=np.full(3, box), grid=(50, 50, 50))
+
+
+def test_sparse_system_empty_cells(oracle):
+    s = _sparse_gas()
+    lb, ub = np.zeros(3), s.box.copy()
+    F0, E0, box, eoff, el = _oracle_forces(oracle, s, grid=s.grid, box_mode=1, lb=lb, ub=ub)
+    ref = oracle.neighbor_pairs(s.pos, box, eoff, el, s.cutoff)
+    ref = ref[np.lexsort((ref[:, 1], ref[:, 0]))]
+    assert len(ref) > 50
+    for prec, tol in ((0, 1e-9), (1, 1e-5)):
+        eng = _engine(s, precision=prec, skin=0.1, rebuild_interval=10, box="explicit", grid=s.grid)
+        F = eng.compute_forces()
+        assert np.isfinite(F).all()
+        assert rel_rms(F, F0) <= tol, (prec, rel_rms(F, F0))
+        assert np.array_equal(eng.pairs(), ref)
+        eng.close()
