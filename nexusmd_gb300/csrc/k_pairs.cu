@@ -163,7 +163,8 @@ __global__ void __launch_bounds__(kHoodWarps * 32) k_build(DevView v) {
     int cap = v.hood_cap;
     float4 *s_q = reinterpret_cast<float4 *>(smem);
     int *s_orig = reinterpret_cast<int *>(s_q + cap);
-    int *s_bnd = s_orig + cap;
+    uint16_t *s_buf = reinterpret_cast<uint16_t *>(s_orig + cap);  // [kHoodWarps][256], 16-byte aligned
+    int *s_bnd = reinterpret_cast<int *>(s_buf + kHoodWarps * 256);
     HoodSpan *spans = reinterpret_cast<HoodSpan *>(s_bnd + 25 * (kRowCells + 1));
     int *s_n = reinterpret_cast<int *>(spans + kMaxSpans);
     int c3f = v.cell3[a0];
@@ -198,23 +199,36 @@ __global__ void __launch_bounds__(kHoodWarps * 32) k_build(DevView v) {
         int ex_lo = ne ? v.excl_lst[e0] : 1, ex_hi = ne ? v.excl_lst[e0 + ne - 1] : 0;
         int count = 0;
         uint16_t *out = v.nl16 + (size_t)i * v.stride;
-        for (int r = 0; r < 25; ++r) {
+        // lane r < 25: the tile range [kb, ke) of row r that i's sphere reaches
+        int kb = 0, ke = 0;
+        if (lane < 25) {
             // distance from i to the row's cell column in x and y
-            float ox = (float)(r / 5 - 2), oy = (float)(r % 5 - 2);
+            float ox = (float)(lane / 5 - 2), oy = (float)(lane % 5 - 2);
             float ddx = fmaxf(fmaxf(ox * csx - pi3[0], pi3[0] - (ox + 1.0f) * csx), 0.0f);
             float ddy = fmaxf(fmaxf(oy * csy - pi3[1], pi3[1] - (oy + 1.0f) * csy), 0.0f);
             float rem = rlm * rlm - (ddx * ddx + ddy * ddy);
-            if (rem < 0.0f) continue;
-            float h = sqrtf(rem) + margin;
-            int zlo = max((int)floorf((pi3[2] - h) * icsz), -2);
-            int zhi = min((int)floorf((pi3[2] + h) * icsz), g + 1);
-            if (zlo > zhi) continue;
-            const int *b = s_bnd + r * (kRowCells + 1);
-            int kb = b[zlo + 2], ke = b[zhi + 3];
-            for (int k0 = kb; k0 < ke; k0 += 32) {
+            if (rem >= 0.0f) {
+                float h = sqrtf(rem) + margin;
+                int zlo = max((int)floorf((pi3[2] - h) * icsz), -2);
+                int zhi = min((int)floorf((pi3[2] + h) * icsz), g + 1);
+                if (zlo <= zhi) {
+                    const int *b = s_bnd + lane * (kRowCells + 1);
+                    kb = b[zlo + 2];
+                    ke = b[zhi + 3];
+                }
+            }
+        }
+        // the current 256-entry chunk of i's list, transposed as in memory
+        uint16_t *buf = s_buf + warp * 256;
+        unsigned rows = __ballot_sync(full, ke > kb);
+        while (rows) {
+            int r = __ffs(rows) - 1;
+            rows &= rows - 1;
+            int rb = __shfl_sync(full, kb, r), re = __shfl_sync(full, ke, r);
+            for (int k0 = rb; k0 < re; k0 += 32) {
                 int k = k0 + lane;
                 bool cand = false;
-                if (k < ke) {
+                if (k < re) {
                     float4 q = s_q[k];
                     float dx = pi3[0] - q.x, dy = pi3[1] - q.y, dz = pi3[2] - q.z;
                     cand = dx * dx + dy * dy + dz * dz < rl2 && k != ki;
@@ -229,13 +243,26 @@ __global__ void __launch_bounds__(kHoodWarps * 32) k_build(DevView v) {
                 }
                 bool ok = cand && !ex;
                 unsigned m = __ballot_sync(full, ok);
-                if (ok) {
-                    int pos = count + __popc(m & ((1u << lane) - 1u));
-                    if (pos < v.stride) out[list_pos(pos)] = (uint16_t)k;
+                int pos = count + __popc(m & ((1u << lane) - 1u));
+                int newc = count + __popc(m);
+                int cend = (count & ~255) + 256;
+                if (ok && pos < cend) buf[list_pos(pos) & 255] = (uint16_t)k;
+                if (newc >= cend) {
+                    // chunk complete: one 16-byte store per lane
+                    __syncwarp();
+                    if (cend <= v.stride)
+                        reinterpret_cast<uint4 *>(out + cend - 256)[lane] = reinterpret_cast<const uint4 *>(buf)[lane];
+                    __syncwarp();
+                    if (ok && pos >= cend) buf[list_pos(pos) & 255] = (uint16_t)k;
                 }
-                count += __popc(m);
+                count = newc;
             }
         }
+        __syncwarp();
+        int cstart = count & ~255;
+        if ((count & 255) && cstart < v.stride)
+            reinterpret_cast<uint4 *>(out + cstart)[lane] = reinterpret_cast<const uint4 *>(buf)[lane];
+        __syncwarp();
         if (lane == 0) {
             v.ncount[i] = count < v.stride ? count : v.stride;
             if (count > v.stride) atomicOr(&v.flags->error, ERR_NLIST_OVERFLOW);
@@ -489,7 +516,8 @@ __global__ void k_collect(DevView v, int sys_sel, int *out, long long cap, unsig
 
 static size_t tail_bytes() { return kMaxSpans * sizeof(HoodSpan) + 4 * sizeof(int); }
 static size_t smem_build(int cap) {
-    return (size_t)cap * (sizeof(float4) + sizeof(int)) + 25 * (kRowCells + 1) * sizeof(int) + tail_bytes();
+    return (size_t)cap * (sizeof(float4) + sizeof(int)) + kHoodWarps * 256 * sizeof(uint16_t) +
+           25 * (kRowCells + 1) * sizeof(int) + tail_bytes();
 }
 static size_t smem_pairs(int cap, int mixed) {
     return mixed ? (size_t)cap * (sizeof(float4) + sizeof(float2)) + tail_bytes() : tail_bytes();
