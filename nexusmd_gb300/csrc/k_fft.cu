@@ -133,7 +133,15 @@ __device__ C *fft_lines(C *a, C *b, int n, int nlines, const int *rad, int np, c
     return a;
 }
 
-__device__ __forceinline__ double grid_value(long long g) { return (double)g * kGridUnscale; }
+// Fixed-point grid word (units of 2^-32) to float without the FP64 pipe:
+// g = hi * 2^24 + lo with lo in [0, 2^24) splits it into two floats that are
+// exact (|g| < 2^47), and their sum is rounded once -- the same float as
+// (float)((double)g * 2^-32).
+__device__ __forceinline__ float grid_value(long long g) {
+    float hi = __int2float_rn((int)(g >> 24)) * 0.00390625f;                         // * 2^-8
+    float lo = __uint2float_rn((unsigned)(g & 0xffffff)) * 2.3283064365386963e-10f;  // * 2^-32
+    return hi + lo;
+}
 __device__ __forceinline__ double grid_value(double g) { return g; }
 
 template <typename C>
@@ -142,7 +150,7 @@ __device__ __forceinline__ const C *tw_table(const DevView &v, int off) {
 }
 
 // ---- z: real -> half spectrum.  Reads the spread accumulator (fixed point
-// in mixed mode) and clears it for the next step.  Two real lines go through
+// in mixed mode; the spread launch clears it first).  Two real lines go through
 // one complex transform (line 2p as the real part, 2p+1 as the imaginary
 // part) and are separated with X_a[k] = (Z[k] + conj Z[n-k]) / 2,
 // X_b[k] = (Z[k] - conj Z[n-k]) / 2i.
@@ -159,19 +167,13 @@ __global__ void k_fft_z_fwd(DevView v, const FftSysDev *fs, const FftWork *work,
     int nl = min(L, nl_total - l0);
     int np2 = (nl + 1) >> 1;  // complex lines
     C *b = a + (L >> 1) * n;
-    Acc *acc = static_cast<Acc *>(v.grid_acc) + F.roff + (long long)l0 * n;
+    const Acc *acc = static_cast<const Acc *>(v.grid_acc) + F.roff + (long long)l0 * n;
     for (int e = threadIdx.x; e < np2 * n; e += blockDim.x) {
         int p = e / n, z = e - p * n;
         int la = 2 * p, lb = 2 * p + 1;
-        Acc ga = acc[(long long)la * n + z];
-        acc[(long long)la * n + z] = (Acc)0;
-        T vb = (T)0;
-        if (lb < nl) {
-            Acc gb = acc[(long long)lb * n + z];
-            acc[(long long)lb * n + z] = (Acc)0;
-            vb = (T)grid_value(gb);
-        }
-        a[e] = Cx<C>::mk((T)grid_value(ga), vb);
+        Acc ga = __ldcs(acc + (long long)la * n + z);
+        Acc gb = lb < nl ? __ldcs(acc + (long long)lb * n + z) : (Acc)0;
+        a[e] = Cx<C>::mk((T)grid_value(ga), (T)grid_value(gb));
     }
     __syncthreads();
     C *res = fft_lines(a, b, n, np2, F.rad[2], F.np[2], tw_table<C>(v, F.tw[2]), -1);

@@ -158,6 +158,8 @@ __global__ void __launch_bounds__(128) k_gather(DevView v, const FftSysDev *fs) 
 void spread_set_smem(int) {}
 
 void launch_spread(const DevView &v, const FftPlan &plan, cudaStream_t st) {
+    // the accumulator (int64 fixed point or double, 8 bytes per point) starts at zero
+    cudaMemsetAsync(v.grid_acc, 0, sizeof(long long) * (size_t)v.total_grid, st);
     int nb = (v.N + 127) / 128;
     if (v.mixed)
         k_spread<float, long long><<<nb, 128, 0, st>>>(v, plan.dsys);
