@@ -73,6 +73,15 @@ typedef struct {
     double box_lb[3], box_ub[3];  /* used when box_from_positions == 0 */
     int32_t force_mask;       /* NXM_FORCE_* bits */
     int32_t exclusion_depth;  /* bonds within which pairs are excluded; 3 in the reference */
+    /* NonbondedForce exceptions in OpenMM's semantics (the reference parses
+     * them, SystemXMLParser.cpp:182-191, and ignores them).  Each pair is
+     * excluded from the Ewald direct sum and reciprocal-corrected like a
+     * bonded exclusion, then interacts by ke*chargeProd/r +
+     * 4 eps ((sigma/r)^12 - (sigma/r)^6): scaled 1-4 pairs, or pure
+     * exclusions when chargeProd = epsilon = 0.  0 exceptions = the reference. */
+    int32_t n_exceptions;
+    const int32_t *exception_atoms;  /* [n_exceptions][2] */
+    const double *exception_params;  /* [n_exceptions][3]: chargeProd (e^2), sigma (nm), epsilon (kJ/mol) */
 } nxm_system_desc;
 
 typedef struct {
@@ -82,6 +91,8 @@ typedef struct {
                                  atom moves more than skin/2); 1 = every step */
     int32_t device;           /* CUDA device ordinal */
     int32_t max_neighbors;    /* list capacity per atom; 0 = from density */
+    int32_t exceptions;       /* Simulate only: 1 = apply the system XML's <Exceptions>
+                                 (OpenMM semantics); 0 = ignore them, as the reference */
 } nxm_options;
 
 /* Energies of one system (kJ/mol) at the last evaluation that computed them. */
@@ -93,6 +104,8 @@ typedef struct {
     double reported_potential; /* the reference's TotalEnergy value: reciprocal energy
                                   replaces the bonded sum when nonbonded is on
                                   (NonbondedForce.cpp:387) */
+    double exception;          /* exception pairs (0 without exceptions); included in both
+                                  potentials above */
 } nxm_energies;
 
 typedef struct nxm_ctx nxm_ctx;

@@ -197,6 +197,12 @@ __global__ void k_remap(DevView v) {
     if (t < v.nex) {
         int2 e = v.ex_orig[t];
         v.ex_slot[t] = make_int2(v.slot_of[e.x], v.slot_of[e.y]);
+        return;
+    }
+    t -= v.nex;
+    if (t < v.nxc) {
+        int2 e = v.xc_orig[t];
+        v.xc_slot[t] = make_int2(v.slot_of[e.x], v.slot_of[e.y]);
     }
 }
 
@@ -207,7 +213,7 @@ void launch_derive_inputs(const DevView &v, cudaStream_t st) {
 }
 
 void launch_remap_terms(const DevView &v, cudaStream_t st) {
-    long long n = (long long)v.nb + v.na + v.nt + v.nex;
+    long long n = (long long)v.nb + v.na + v.nt + v.nex + v.nxc;
     if (n > 0) k_remap<<<blocks(n, 256), 256, 0, st>>>(v);
 }
 
@@ -220,7 +226,7 @@ void launch_nlist_rebuild(const DevView &v, cudaStream_t st) {
     k_permute_gather<<<blocks(v.N, 256), 256, 0, st>>>(v);
     k_permute_scatter<<<blocks(v.N, 256), 256, 0, st>>>(v);
     k_derive<<<blocks(v.N, 256), 256, 0, st>>>(v, 1);
-    long long nt = (long long)v.nb + v.na + v.nt + v.nex;
+    long long nt = (long long)v.nb + v.na + v.nt + v.nex + v.nxc;
     if (nt > 0) k_remap<<<blocks(nt, 256), 256, 0, st>>>(v);
     launch_build(v, st);
 }

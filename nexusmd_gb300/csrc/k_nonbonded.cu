@@ -69,6 +69,73 @@ __global__ void __launch_bounds__(256) k_exclusions(DevView v, int energy) {
     if (energy) energy_add(v.E, sys, E_EXCL, e);
 }
 
+// Exception pairs (scaled 1-4 interactions), one thread per pair, in the
+// semantics of OpenMM's NonbondedForce exceptions -- the reference parses
+// them (core/common/src/SystemXMLParser.cpp:182-191) but applies none:
+// E = ke chargeProd / r + 4 eps ((sig/r)^12 - (sig/r)^6) with plain
+// Coulomb.  Every exception pair is also an exclusion, so the Ewald sum
+// already left it out of the direct space and the exclusion correction
+// removed its reciprocal part.  FP64 displacement with the reference's
+// minimum image; FP32 arithmetic and fixed-point sums in mixed mode.
+template <bool MIXED>
+__global__ void __launch_bounds__(256) k_exceptions(DevView v, int energy) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0.0;
+    int sys = 0;
+    if (t < v.nxc) {
+        int2 p = v.xc_slot[t];
+        int ii = p.x, jj = p.y;
+        sys = v.sys_of[ii];
+        const SysDev &S = v.sys[sys];
+        double4 prm = v.xc_prm[t];
+        double dx = min_image(v.x[ii] - v.x[jj], S.L[0], S.halfL[0]);
+        double dy = min_image(v.y[ii] - v.y[jj], S.L[1], S.halfL[1]);
+        double dz = min_image(v.z[ii] - v.z[jj], S.L[2], S.halfL[2]);
+        if (MIXED) {
+            float fdx = (float)dx, fdy = (float)dy, fdz = (float)dz;
+            float rinv2 = 1.0f / (fdx * fdx + fdy * fdy + fdz * fdz);
+            float rinv = sqrtf(rinv2);
+            float coul = (float)prm.x * rinv;
+            float s2 = (float)(prm.y * prm.y) * rinv2;
+            float s6 = s2 * s2 * s2;
+            float e4 = (float)prm.z;
+            float dEdR = (coul + e4 * (12.0f * s6 - 6.0f) * s6) * rinv2;
+            acc_add(static_cast<long long *>(v.fx) + ii, fdx * dEdR);
+            acc_add(static_cast<long long *>(v.fy) + ii, fdy * dEdR);
+            acc_add(static_cast<long long *>(v.fz) + ii, fdz * dEdR);
+            acc_add(static_cast<long long *>(v.fx) + jj, -fdx * dEdR);
+            acc_add(static_cast<long long *>(v.fy) + jj, -fdy * dEdR);
+            acc_add(static_cast<long long *>(v.fz) + jj, -fdz * dEdR);
+            e = (double)coul + (double)(e4 * (s6 - 1.0f) * s6);
+        } else {
+            double r2 = dx * dx + dy * dy + dz * dz;
+            double rinv = 1.0 / sqrt(r2);
+            double coul = prm.x * rinv;
+            double s2 = prm.y * rinv;
+            s2 *= s2;
+            double s6 = s2 * s2 * s2;
+            double dEdR = (coul + prm.z * (12.0 * s6 - 6.0) * s6) * rinv * rinv;
+            atomicAdd(static_cast<double *>(v.fx) + ii, dx * dEdR);
+            atomicAdd(static_cast<double *>(v.fy) + ii, dy * dEdR);
+            atomicAdd(static_cast<double *>(v.fz) + ii, dz * dEdR);
+            atomicAdd(static_cast<double *>(v.fx) + jj, -dx * dEdR);
+            atomicAdd(static_cast<double *>(v.fy) + jj, -dy * dEdR);
+            atomicAdd(static_cast<double *>(v.fz) + jj, -dz * dEdR);
+            e = coul + prm.z * (s6 - 1.0) * s6;
+        }
+    }
+    if (energy) energy_add(v.E, sys, E_EXCEPT, e);
+}
+
+void launch_exceptions(const DevView &v, int energy, cudaStream_t st) {
+    if (v.nxc == 0) return;
+    int nb = (v.nxc + 255) / 256;
+    if (v.mixed)
+        k_exceptions<true><<<nb, 256, 0, st>>>(v, energy);
+    else
+        k_exceptions<false><<<nb, 256, 0, st>>>(v, energy);
+}
+
 void launch_exclusions(const DevView &v, int energy, cudaStream_t st) {
     if (v.nex == 0) return;
     int nb = (v.nex + 255) / 256;

@@ -92,6 +92,12 @@ int nxm_create(const nxm_system_desc *systems, int32_t n_systems, const nxm_opti
         h.box_from_positions = d.box_from_positions;
         h.force_mask = d.force_mask;
         h.excl_depth = d.exclusion_depth;
+        if (d.n_exceptions < 0 || (d.n_exceptions > 0 && (!d.exception_atoms || !d.exception_params)))
+            return fail(NXM_ERR_INVALID, "nxm_create: exception count without arrays");
+        if (d.n_exceptions > 0) {
+            h.exc.assign(d.exception_atoms, d.exception_atoms + 2 * (size_t)d.n_exceptions);
+            h.exc_prm.assign(d.exception_params, d.exception_params + 3 * (size_t)d.n_exceptions);
+        }
     }
     nxm_ctx *c = new (std::nothrow) nxm_ctx;
     if (!c) return fail(NXM_ERR_INVALID, "out of host memory");

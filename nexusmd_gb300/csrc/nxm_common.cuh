@@ -47,6 +47,8 @@ enum EnergyTerm {
     E_VDW,
     E_EXCL,
     E_KIN,
+    E_EXCEPT,  // exception (scaled 1-4) pairs
+
     E_SLOTS = 16
 };
 

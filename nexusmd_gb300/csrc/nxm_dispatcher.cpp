@@ -83,6 +83,14 @@ public:
         nxm_options opt;
         nxm_default_options(&opt);
         if (have_options) opt = options;
+        if (opt.exceptions && nonbondedForceEnabled) {
+            // <Exceptions> of the system XML in OpenMM semantics (the reference ignores them)
+            for (auto &x : ps.nb.exceptions) {
+                h.exc.push_back(x.p1);
+                h.exc.push_back(x.p2);
+                h.exc_prm.insert(h.exc_prm.end(), {x.q, x.sig, x.eps});
+            }
+        }
         auto eng = std::make_unique<nxm::Engine>();
         std::string err = eng->init({h}, opt, ps.positions.data());
         if (!err.empty()) throw std::runtime_error(err);

@@ -198,6 +198,8 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     plan_.hsys.assign(S, FftSysDev{});
     std::vector<std::vector<int>> excl_all(N_);
     std::vector<int2> ex_pairs;
+    std::vector<int2> xc_pairs;      // exception pairs, batch-global original indices
+    std::vector<double4> xc_prm;
     int off = 0, cell_off = 0;
     long long roff = 0, coff = 0;
     int tw_total = 0;
@@ -292,6 +294,24 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         std::vector<std::vector<int>> ex;
         std::string err = exclusions(h, ex);
         if (!err.empty()) return err;
+        // exception pairs are excluded from the Ewald direct sum too
+        if (h.exc.size() != 2 * (h.exc_prm.size() / 3)) return "exception arrays disagree in length";
+        for (size_t k = 0; k < h.exc.size() / 2; ++k) {
+            int a = h.exc[2 * k], b = h.exc[2 * k + 1];
+            if (a < 0 || b < 0 || a >= h.n || b >= h.n || a == b) return "exception: illegal particle index";
+            ex[a].push_back(b);
+            ex[b].push_back(a);
+            if (h.force_mask & NXM_FORCE_NONBONDED) {
+                xc_pairs.push_back(make_int2(off + a, off + b));
+                const double *p = &h.exc_prm[3 * k];
+                xc_prm.push_back(make_double4(kOne4PiEps0 * p[0], p[1], 4.0 * p[2], 0.0));
+            }
+        }
+        if (!h.exc.empty())
+            for (auto &l : ex) {
+                std::sort(l.begin(), l.end());
+                l.erase(std::unique(l.begin(), l.end()), l.end());
+            }
         for (int i = 0; i < h.n; ++i) {
             for (int j : ex[i]) {
                 excl_all[off + i].push_back(off + j);
@@ -518,6 +538,14 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     v_.ex_orig = dalloc<int2>(v_.nex);
     v_.ex_slot = dalloc<int2>(v_.nex);
     if (v_.nex) up(v_.ex_orig, ex_pairs.data(), sizeof(int2) * v_.nex);
+    v_.nxc = (int)xc_pairs.size();
+    v_.xc_orig = dalloc<int2>(v_.nxc);
+    v_.xc_slot = dalloc<int2>(v_.nxc);
+    v_.xc_prm = dalloc<double4>(v_.nxc);
+    if (v_.nxc) {
+        up(v_.xc_orig, xc_pairs.data(), sizeof(int2) * v_.nxc);
+        up(v_.xc_prm, xc_prm.data(), sizeof(double4) * v_.nxc);
+    }
 
     // ---- PME
     bool any_nb = false;
@@ -690,7 +718,7 @@ std::string Engine::set_velocities(const double *xyz) {
 // Kernel launches of force_launches below, without launching.
 static int force_launch_count(const DevView &v) {
     int n = (v.nb + v.na + v.nt) ? 1 : 0;
-    if (v.force_mask & NXM_FORCE_NONBONDED) n += 1 + (v.nex ? 1 : 0) + 7;
+    if (v.force_mask & NXM_FORCE_NONBONDED) n += 1 + (v.nex ? 1 : 0) + (v.nxc ? 1 : 0) + 7;
     return n;
 }
 
@@ -705,6 +733,10 @@ static int force_launches(const DevView &v, const FftPlan &plan, int energy, cud
         ++n;
         if (v.nex) {
             launch_exclusions(v, energy, st);
+            ++n;
+        }
+        if (v.nxc) {
+            launch_exceptions(v, energy, st);
             ++n;
         }
         launch_pme(v, plan, energy, st);
@@ -883,6 +915,7 @@ std::string Engine::profile(int nsteps, double dt, double *ms) {
         if (nb) launch_pairs(v_, 0, st_);
         cudaEventRecord(ev[3], st_);
         if (nb && v_.nex) launch_exclusions(v_, 0, st_);
+        if (nb && v_.nxc) launch_exceptions(v_, 0, st_);
         cudaEventRecord(ev[4], st_);
         if (nb && plan_.nz) launch_spread(v_, plan_, st_);
         cudaEventRecord(ev[5], st_);
@@ -956,14 +989,17 @@ void Engine::energies(int s, nxm_energies *out) const {
         out->coulomb = e[E_COUL];
         out->vdw = e[E_VDW];
         out->exclusion = e[E_EXCL];
-        double nb = out->recip + out->self + out->coulomb + out->vdw - out->exclusion;
+        out->exception = e[E_EXCEPT];
+        double nb = out->recip + out->self + out->coulomb + out->vdw - out->exclusion + out->exception;
         pe += nb;
         // NonbondedForce.cpp:387 assigns the reciprocal energy to the running
         // total, then self, direct and exclusion terms are added to it
+        // (exceptions, which the reference never applies, come last)
         reported = out->recip;
         reported += out->self;
         reported += out->coulomb + out->vdw;
         reported -= out->exclusion;
+        reported += out->exception;
     }
     out->potential = pe;
     out->reported_potential = reported;

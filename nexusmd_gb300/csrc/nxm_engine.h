@@ -26,6 +26,9 @@ struct HostSystem {
     double lb[3] = {0, 0, 0}, ub[3] = {0, 0, 0};
     int force_mask = 15;
     int excl_depth = 3;
+    // exception pairs (OpenMM semantics): atoms, and chargeProd / sigma / epsilon
+    std::vector<int> exc;
+    std::vector<double> exc_prm;
 };
 
 struct SysHost {

@@ -61,6 +61,9 @@ struct DevView {
     int *tors_per;
     int nex;
     int2 *ex_orig, *ex_slot;   // excluded pairs (i < j by original index)
+    int nxc;                   // exception pairs (OpenMM semantics), also excluded
+    int2 *xc_orig, *xc_slot;
+    double4 *xc_prm;           // ke * chargeProd, sigma, 4 epsilon, 0
     int *bond_sys, *angle_sys, *tors_sys, *ex_sys;
     // PME
     long long total_grid, total_cgrid;
@@ -88,6 +91,7 @@ void launch_derive_inputs(const DevView &v, cudaStream_t st);
 void launch_bonded(const DevView &v, int energy, cudaStream_t st);
 void launch_pairs(const DevView &v, int energy, cudaStream_t st);
 void launch_exclusions(const DevView &v, int energy, cudaStream_t st);
+void launch_exceptions(const DevView &v, int energy, cudaStream_t st);
 void launch_pme(const DevView &v, const struct FftPlan &plan, int energy, cudaStream_t st);
 void launch_spread(const DevView &v, const struct FftPlan &plan, cudaStream_t st);
 void launch_fft_convolve(const DevView &v, const struct FftPlan &plan, int energy, cudaStream_t st);

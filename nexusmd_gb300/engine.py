@@ -34,18 +34,20 @@ class SystemDesc(C.Structure):
                 ("use_switching", C.c_int32), ("switching_distance", C.c_double),
                 ("grid", C.c_int32 * 3), ("box_from_positions", C.c_int32),
                 ("box_lb", C.c_double * 3), ("box_ub", C.c_double * 3),
-                ("force_mask", C.c_int32), ("exclusion_depth", C.c_int32)]
+                ("force_mask", C.c_int32), ("exclusion_depth", C.c_int32),
+                ("n_exceptions", C.c_int32), ("exception_atoms", C.c_void_p),
+                ("exception_params", C.c_void_p)]
 
 
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("skin", C.c_double), ("rebuild_interval", C.c_int32),
-                ("device", C.c_int32), ("max_neighbors", C.c_int32)]
+                ("device", C.c_int32), ("max_neighbors", C.c_int32), ("exceptions", C.c_int32)]
 
 
 class Energies(C.Structure):
     _fields_ = [(k, C.c_double) for k in
                 ("bond", "angle", "torsion", "recip", "self", "coulomb", "vdw", "exclusion",
-                 "kinetic", "potential", "reported_potential")]
+                 "kinetic", "potential", "reported_potential", "exception")]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -111,10 +113,12 @@ class Engine:
 
     def __init__(self, systems, precision=PRECISION_MIXED, skin=0.1, rebuild_interval=10,
                  force_mask=FORCE_ALL, box="reference", grid=None, use_switch=0,
-                 switch_dist=0.0, exclusion_depth=3, max_neighbors=0, device=0):
+                 switch_dist=0.0, exclusion_depth=3, max_neighbors=0, device=0, exceptions=False):
         """``box``: "reference" (extent + 1%, as the reference) or "explicit"
         (each system's periodic box [0, L)); ``grid``: None = each system's
-        ``grid`` attribute, (0,0,0) = the reference's power-of-two rule."""
+        ``grid`` attribute, (0,0,0) = the reference's power-of-two rule;
+        ``exceptions``: pass each system's ``exc_idx`` / ``exc_prm`` exception
+        pairs (OpenMM semantics) when it has them."""
         L = load_library()
         if not isinstance(systems, (list, tuple)):
             systems = [systems]
@@ -150,6 +154,11 @@ class Engine:
                     d.box_lb[i], d.box_ub[i] = 0.0, float(s.box[i])
             d.force_mask = int(force_mask)
             d.exclusion_depth = int(exclusion_depth)
+            if exceptions and getattr(s, "exc_idx", None) is not None and len(s.exc_idx):
+                k["xi"] = _arr(s.exc_idx, np.int32)
+                k["xp"] = _arr(s.exc_prm, np.float64)
+                d.n_exceptions = len(k["xi"])
+                d.exception_atoms, d.exception_params = k["xi"].ctypes.data, k["xp"].ctypes.data
             pos.append(_arr(s.pos, np.float64))
         self.n_atoms = int(sum(s.n for s in systems))
         opt = Options()

@@ -68,6 +68,10 @@ class System:
     res_name: Optional[list] = None
     atom_name: Optional[list] = None
     res_seq: Optional[np.ndarray] = None
+    # NonbondedForce exceptions (OpenMM semantics): pairs and
+    # [chargeProd e^2, sigma nm, epsilon kJ/mol]; None = none
+    exc_idx: Optional[np.ndarray] = None
+    exc_prm: Optional[np.ndarray] = None
 
     @property
     def n(self) -> int:
@@ -510,12 +514,36 @@ def subset(s: System, keep: np.ndarray) -> System:
     a, ap = terms(s.angles, s.angle_prm)
     t, tp, tn = terms(s.torsions, s.torsion_prm, s.torsion_n)
     pick = lambda lst: [lst[i] for i in keep] if lst is not None else None
+    xi = xp = None
+    if s.exc_idx is not None:
+        xi, xp = terms(np.asarray(s.exc_idx), np.asarray(s.exc_prm))
     return dataclasses.replace(
         s, pos=s.pos[keep].copy(), mass=s.mass[keep].copy(), charge=s.charge[keep].copy(),
         sigma=s.sigma[keep].copy(), epsilon=s.epsilon[keep].copy(), bonds=b, bond_prm=bp,
         angles=a, angle_prm=ap, torsions=t, torsion_prm=tp, torsion_n=tn,
         res_name=pick(s.res_name), atom_name=pick(s.atom_name),
-        res_seq=s.res_seq[keep].copy() if s.res_seq is not None else None)
+        res_seq=s.res_seq[keep].copy() if s.res_seq is not None else None, exc_idx=xi, exc_prm=xp)
+
+
+COULOMB14 = 1.0 / 1.2  # 0.8333, the AMBER-style 1-4 Coulomb scale
+LJ14 = 0.5
+
+
+def with_exceptions(s: System, coulomb14: float = COULOMB14, lj14: float = LJ14) -> System:
+    """The system with its 1-4 pairs as scaled exceptions, the way OpenMM's
+    NonbondedForce.createExceptionsFromBonds makes them: chargeProd =
+    coulomb14 q_i q_j, sigma = (sigma_i + sigma_j) / 2, epsilon = lj14
+    sqrt(eps_i eps_j).  1-4 pairs are the end atoms of the torsions (the
+    chains here have no rings, so no pair is also 1-2 or 1-3)."""
+    if len(s.torsions):
+        p = np.sort(np.asarray(s.torsions)[:, [0, 3]], axis=1)
+        p = np.unique(p, axis=0).astype(np.int32)
+    else:
+        p = np.zeros((0, 2), np.int32)
+    i, j = p[:, 0], p[:, 1]
+    prm = np.stack([coulomb14 * s.charge[i] * s.charge[j], 0.5 * (s.sigma[i] + s.sigma[j]),
+                    lj14 * np.sqrt(s.epsilon[i] * s.epsilon[j])], axis=1) if len(p) else np.zeros((0, 3))
+    return dataclasses.replace(s, exc_idx=p, exc_prm=prm)
 
 
 # ---------------------------------------------------------------------------
@@ -562,7 +590,13 @@ def write_system_xml(s: System, path: str, use_switch: bool = False, switch_dist
     out += ['\t\t\t\t<Particle eps="%.17g" q="%.17g" sig="%.17g"/>' % (e, c, g)
             for c, g, e in zip(s.charge, s.sigma, s.epsilon)]
     out.append('\t\t\t</Particles>')
-    out.append('\t\t\t<Exceptions/>')
+    if s.exc_idx is not None and len(s.exc_idx):
+        out.append('\t\t\t<Exceptions>')
+        out += ['\t\t\t\t<Exception eps="%.17g" p1="%d" p2="%d" q="%.17g" sig="%.17g"/>' % (p[2], e[0], e[1], p[0], p[1])
+                for e, p in zip(s.exc_idx, s.exc_prm)]
+        out.append('\t\t\t</Exceptions>')
+    else:
+        out.append('\t\t\t<Exceptions/>')
     out += ['\t\t</Force>', '\t</Forces>', '</System>']
     with open(path, "w") as f:
         f.write("\n".join(out) + "\n")

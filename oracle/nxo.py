@@ -47,7 +47,7 @@ class Box(C.Structure):
 class Energy(C.Structure):
     _fields_ = [(k, C.c_double) for k in
                 ("bond", "angle", "torsion", "recip", "self", "coulomb", "vdw", "exclusion",
-                 "reported_pe")]
+                 "reported_pe", "exception")]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -62,7 +62,8 @@ class SystemDesc(C.Structure):
                 ("cutoff", C.c_double), ("ewald_tol", C.c_double), ("use_switch", C.c_int),
                 ("switch_dist", C.c_double), ("switch_quirk", C.c_int), ("grid", C.c_int * 3),
                 ("box_mode", C.c_int), ("lb", C.c_double * 3), ("ub", C.c_double * 3),
-                ("force_mask", C.c_int), ("exclusion_depth", C.c_int)]
+                ("force_mask", C.c_int), ("exclusion_depth", C.c_int), ("nexc", C.c_int),
+                ("exc_idx", C.c_void_p), ("exc_prm", C.c_void_p)]
 
 
 class Timing(C.Structure):
@@ -111,6 +112,8 @@ class Oracle:
         L.nxo_run_timed.argtypes = [C.POINTER(SystemDesc), _dp, _dp, C.c_double, C.c_int,
                                     C.POINTER(Timing)]
         L.nxo_fft3d.argtypes = [_dp, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.nxo_exceptions.argtypes = [_dp, C.c_int, _ip, _dp, C.POINTER(Box), _dp]
+        L.nxo_exceptions.restype = C.c_double
 
     # -- geometry
     def box_from_positions(self, pos) -> Box:
@@ -167,6 +170,30 @@ class Oracle:
                 return off, lst[:ne].copy()
             cap = -ne
 
+    @staticmethod
+    def union_exclusions(off, lst, exc_idx):
+        """Exclusion CSR united with exception pairs (both directions),
+        partners ascending and unique."""
+        n = len(off) - 1
+        parts = [set(lst[off[i]:off[i + 1]].tolist()) for i in range(n)]
+        for a, b in np.asarray(exc_idx, np.int64).reshape(-1, 2):
+            parts[a].add(int(b))
+            parts[b].add(int(a))
+        noff = np.zeros(n + 1, np.int32)
+        out = []
+        for i in range(n):
+            p = sorted(parts[i])
+            out.extend(p)
+            noff[i + 1] = noff[i] + len(p)
+        return noff, np.array(out, np.int32)
+
+    def exceptions(self, pos, idx, prm, box):
+        """Exception pairs in OpenMM semantics: (energy, forces)."""
+        F = np.zeros((len(pos), 3))
+        E = self.lib.nxo_exceptions(_c(pos, np.float64), len(idx), _c(idx, np.int32), _c(prm, np.float64),
+                                    C.byref(box), F)
+        return E, F
+
     def neighbor_pairs(self, pos, box, eoff, elst, cutoff):
         p = _c(pos, np.float64)
         cap = 300 * len(p) + 1024
@@ -203,8 +230,9 @@ class Oracle:
 
     # -- whole system
     def describe(self, s, force_mask=15, box_mode=0, lb=None, ub=None, grid=None,
-                 use_switch=0, switch_dist=0.0, switch_quirk=1, exclusion_depth=3):
-        """SystemDesc for a synthetic.System (keeps the arrays alive on the desc)."""
+                 use_switch=0, switch_dist=0.0, switch_quirk=1, exclusion_depth=3, exceptions=None):
+        """SystemDesc for a synthetic.System (keeps the arrays alive on the desc).
+        exceptions: None, or (idx m x 2, prm m x 3: chargeProd, sigma, epsilon)."""
         keep = dict(mass=_c(s.mass, np.float64), q=_c(s.charge, np.float64),
                     sig=_c(s.sigma, np.float64), eps=_c(s.epsilon, np.float64),
                     bonds=_c(s.bonds, np.int32), bond_prm=_c(s.bond_prm, np.float64),
@@ -227,6 +255,11 @@ class Oracle:
                 d.lb[k], d.ub[k] = lb[k], ub[k]
         d.force_mask = force_mask
         d.exclusion_depth = exclusion_depth
+        if exceptions is not None and len(exceptions[0]):
+            keep["exc_idx"] = _c(exceptions[0], np.int32)
+            keep["exc_prm"] = _c(exceptions[1], np.float64)
+            d.nexc = len(keep["exc_idx"])
+            d.exc_idx, d.exc_prm = keep["exc_idx"].ctypes.data, keep["exc_prm"].ctypes.data
         d._keep = keep
         return d
 

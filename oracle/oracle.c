@@ -731,6 +731,35 @@ int nxo_nonbonded(const nxo_system *s, const double *pos, const nxo_box *box, co
     return 0;
 }
 
+/* Exceptions, OpenMM semantics (the reference has no code for them): one
+ * pass over the listed pairs, d = p_i - p_j with the reference's minimum
+ * image, dE/dR / r applied as in direct_pairs above. */
+double nxo_exceptions(const double *pos, int nexc, const int *idx, const double *prm, const nxo_box *box,
+                      double *F) {
+    double e = 0.0;
+    for (int k = 0; k < nexc; ++k) {
+        int ii = idx[2 * k], jj = idx[2 * k + 1];
+        double qq = prm[3 * k], sig = prm[3 * k + 1], eps = prm[3 * k + 2];
+        double d[3];
+        nxo_min_image(pos + 3 * ii, pos + 3 * jj, box, d);
+        double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        double inverseR = 1.0 / sqrt(r2);
+        double coul = ONE_4PI_EPS0_ * qq * inverseR;
+        double s2 = sig * inverseR;
+        s2 *= s2;
+        double s6 = s2 * s2 * s2;
+        double lj = 4.0 * eps * (s6 - 1.0) * s6;
+        double dEdR = (coul + 4.0 * eps * (12.0 * s6 - 6.0) * s6) * inverseR * inverseR;
+        for (int c = 0; c < 3; ++c) {
+            double f = d[c] * dEdR;
+            F[3 * ii + c] += f;
+            F[3 * jj + c] -= f;
+        }
+        e += coul + lj;
+    }
+    return e;
+}
+
 /* Engine.cpp:75-95.  reported_pe reproduces the reference's bookkeeping:
  * reciprocalConvolutionAndEnergy *assigns* the reciprocal energy to the
  * running total (NonbondedForce.cpp:387 via :489), which drops the bonded
@@ -758,6 +787,10 @@ int nxo_forces(const nxo_system *s, const double *pos, const nxo_box *box, const
         pe += E->self;
         pe += E->coulomb + E->vdw;
         pe -= E->exclusion;
+        if (s->nexc > 0) {
+            E->exception = nxo_exceptions(pos, s->nexc, s->exc_idx, s->exc_prm, box, F);
+            pe += E->exception;
+        }
     }
     E->reported_pe = pe;
     return 0;
@@ -801,6 +834,49 @@ double nxo_kinetic(int n, const double *vel, const double *mass, const double *F
     return total;
 }
 
+/* Exclusion CSR united with the exception pairs (both directions), each
+ * atom's partners ascending and unique.  Replaces *eoff / *elst. */
+static void merge_exceptions(const nxo_system *s, int **eoff, int **elst) {
+    int n = s->n;
+    int *cnt = (int *)calloc((size_t)n + 1, sizeof(int));
+    for (int i = 0; i < n; ++i) cnt[i] = (*eoff)[i + 1] - (*eoff)[i];
+    for (int k = 0; k < s->nexc; ++k) {
+        cnt[s->exc_idx[2 * k]]++;
+        cnt[s->exc_idx[2 * k + 1]]++;
+    }
+    int *off = (int *)malloc(sizeof(int) * ((size_t)n + 1));
+    off[0] = 0;
+    for (int i = 0; i < n; ++i) off[i + 1] = off[i] + cnt[i];
+    int *lst = (int *)malloc(sizeof(int) * (size_t)(off[n] > 0 ? off[n] : 1));
+    for (int i = 0; i < n; ++i) {
+        cnt[i] = (*eoff)[i + 1] - (*eoff)[i];
+        memcpy(lst + off[i], *elst + (*eoff)[i], sizeof(int) * (size_t)cnt[i]);
+    }
+    for (int k = 0; k < s->nexc; ++k) {
+        int a = s->exc_idx[2 * k], b = s->exc_idx[2 * k + 1];
+        lst[off[a] + cnt[a]++] = b;
+        lst[off[b] + cnt[b]++] = a;
+    }
+    /* sort and compact each atom's partners */
+    int w = 0;
+    int *noff = (int *)malloc(sizeof(int) * ((size_t)n + 1));
+    for (int i = 0; i < n; ++i) {
+        qsort(lst + off[i], (size_t)cnt[i], sizeof(int), cmp_int);
+        noff[i] = w;
+        for (int e = 0; e < cnt[i]; ++e) {
+            int v = lst[off[i] + e];
+            if (e == 0 || v != lst[off[i] + e - 1]) lst[w++] = v;
+        }
+    }
+    noff[n] = w;
+    free(*eoff);
+    free(*elst);
+    free(cnt);
+    free(off);
+    *eoff = noff;
+    *elst = lst;
+}
+
 static int setup(const nxo_system *s, const double *pos, nxo_box *box, int **eoff, int **elst,
                  double **invm) {
     if (s->box_mode == 0)
@@ -820,6 +896,7 @@ static int setup(const nxo_system *s, const double *pos, nxo_box *box, int **eof
         if (ne == -1) return -1;
         cap = -ne;
     }
+    if (s->nexc > 0 && (s->force_mask & 8)) merge_exceptions(s, eoff, elst);
     /* VerletIntegration.cpp:37-45 */
     *invm = (double *)malloc(sizeof(double) * (size_t)s->n);
     for (int i = 0; i < s->n; ++i) (*invm)[i] = (s->mass[i] == 0.0) ? 0.0 : 1.0 / s->mass[i];

@@ -23,6 +23,7 @@ typedef struct {
     double bond, angle, torsion;
     double recip, self, coulomb, vdw, exclusion;
     double reported_pe; /* what the reference puts in totalPEnergy */
+    double exception;   /* scaled 1-4 (exception) pairs; 0 without exceptions */
 } nxo_energy;
 
 typedef struct {
@@ -47,6 +48,12 @@ typedef struct {
     double lb[3], ub[3];
     int force_mask; /* 1 bond, 2 angle, 4 torsion, 8 nonbonded */
     int exclusion_depth;
+    /* NonbondedForce exceptions (OpenMM semantics; the reference parses them,
+     * SystemXMLParser.cpp:182-191, but never applies them).  Each pair must
+     * also be in the exclusion CSR the caller passes. */
+    int nexc;
+    const int *exc_idx;    /* nexc x 2 */
+    const double *exc_prm; /* nexc x 3: chargeProd (e^2), sigma (nm), epsilon (kJ/mol) */
 } nxo_system;
 
 /* PeriodicBoundaryCondition.cpp:11-88 / :93-104 */
@@ -83,6 +90,14 @@ void nxo_bspline_moduli(int K, double *mod);
 /* the charge grid Q after spreading (NonbondedForce.cpp:220-260), complex interleaved */
 void nxo_spread(int n, const double *pos, const double *q, const nxo_box *box, const int grid[3],
                 double *grid_out);
+
+/* Exception pairs in OpenMM's NonbondedForce semantics (no counterpart in
+ * the reference): E = ke chargeProd / r + 4 eps ((sig/r)^12 - (sig/r)^6),
+ * plain Coulomb (the pair is excluded from the Ewald sum and its reciprocal
+ * part removed by the exclusion correction), reference minimum image.
+ * Returns the energy, adds forces into F[n][3]. */
+double nxo_exceptions(const double *pos, int nexc, const int *idx, const double *prm, const nxo_box *box,
+                      double *F);
 
 /* Whole NonbondedForce::calculateForces (NonbondedForce.cpp:633-647). */
 int nxo_nonbonded(const nxo_system *s, const double *pos, const nxo_box *box, const int *eoff,

@@ -199,3 +199,43 @@ def test_sparse_system_empty_cells(oracle):
         assert rel_rms(F, F0) <= tol, (prec, rel_rms(F, F0))
         assert np.array_equal(eng.pairs(), ref)
         eng.close()
+
+
+@pytest.mark.parametrize("depth", [3, 2])
+def test_exceptions_physics_mode(oracle, depth):
+    """Scaled 1-4 exceptions (OpenMM semantics) vs the oracle.  With depth 2
+    the 1-4 pairs are excluded only because they are exceptions, so the
+    engine's union of bonded exclusions and exception pairs is exercised."""
+    s = sy.with_exceptions(sy.config_system(1))
+    lb, ub = np.zeros(3), s.box.copy()
+    box = oracle.box_explicit(lb, ub)
+    off, lst = oracle.exclusions(s.n, s.bonds, depth=depth)
+    off, lst = oracle.union_exclusions(off, lst, s.exc_idx)
+    d = oracle.describe(s, box_mode=1, lb=lb, ub=ub, exclusion_depth=depth, exceptions=(s.exc_idx, s.exc_prm))
+    F0, E0 = oracle.forces(d, s.pos, box, off, lst)
+    assert E0["exception"] != 0.0
+    scale = max(abs(E0[k]) for k in TERMS)
+    for prec, tol in ((0, 1e-9), (1, 1e-5)):
+        eng = _engine(s, precision=prec, skin=0.1, rebuild_interval=10, box="explicit", exclusion_depth=depth,
+                      exceptions=True)
+        F = eng.compute_forces()
+        E = eng.energies()
+        assert rel_rms(F, F0) <= tol, (prec, depth, rel_rms(F, F0))
+        etol = 1e-9 if prec == 0 else 2e-5
+        for k in TERMS + ("exception",):
+            assert abs(E[k] - E0[k]) <= etol * scale + 1e-6, (prec, k, E[k], E0[k])
+        assert abs(E["potential"] - (E0["bond"] + E0["angle"] + E0["torsion"] + E0["recip"] + E0["self"]
+                                     + E0["coulomb"] + E0["vdw"] - E0["exclusion"] + E0["exception"])) \
+            <= etol * scale + 1e-6
+        eng.close()
+
+
+def test_exceptions_bit_reproducible():
+    s = sy.with_exceptions(sy.config_system(1))
+    outs = []
+    for _ in range(2):
+        eng = _engine(s, precision=1, skin=0.1, rebuild_interval=10, box="explicit", exceptions=True)
+        eng.step(5, 0.0005)
+        outs.append(eng.forces())
+        eng.close()
+    assert np.array_equal(outs[0], outs[1])

@@ -79,3 +79,39 @@ def test_simulate_mixed_precision_tracks_reference(tmp_path):
     pvf, rpvf = got["PVFReportout0.pdb"], _gold("PVFReportout0.pdb")
     assert len(pvf) == len(rpvf)
     assert all(NUM.sub("#", x) == NUM.sub("#", y) for x, y in zip(pvf, rpvf))
+
+
+def test_simulate_applies_xml_exceptions_on_request(tmp_path, oracle):
+    """SetOptions(exceptions=True): the system XML's <Exceptions> (scaled
+    1-4 pairs) enter the run; the step-0 potential in TotalEnergy equals the
+    oracle's in the same mode, and without the option the file is the
+    reference's (exceptions ignored)."""
+    import NexusMD
+    from nexusmd_gb300 import synthetic as sy
+    s = sy.with_exceptions(sy.compat_system(sy.make_system(1, 4, 100, 2.8, seed=21)))
+    sp, st, pdb = sy.write_inputs(s, str(tmp_path), "exc")
+    pe = {}
+    for use in (False, True):
+        d = NexusMD.TaskDispatcher.CreateDispatcher("GPU")
+        d.EnableHarmonicBondForce()
+        d.EnableHarmonicAngleForce()
+        d.EnablePeriodicTorsionForce()
+        d.EnableNonbondedForce()
+        d.SetOptions(precision="fp64", exceptions=use)
+        cwd = os.getcwd()
+        os.chdir(tmp_path)
+        try:
+            d.Simulate(sp, st, pdb, "o%d.pdb" % use, 0.0005, 1, 1)
+            line = open(os.path.join(tmp_path, "TotalEnergyo%d.pdb" % use)).read().splitlines()[1]
+        finally:
+            os.chdir(cwd)
+        pe[use] = float(line.split()[2])
+    box = oracle.box_from_positions(s.pos)
+    off, lst = oracle.exclusions(s.n, s.bonds)
+    off, lst = oracle.union_exclusions(off, lst, s.exc_idx)
+    ref_off = oracle.describe(s)
+    _, E0 = oracle.forces(ref_off, s.pos, box, off, lst)
+    _, E1 = oracle.forces(oracle.describe(s, exceptions=(s.exc_idx, s.exc_prm)), s.pos, box, off, lst)
+    assert E1["exception"] != 0.0
+    assert abs(pe[False] - E0["reported_pe"]) <= 1e-8 * abs(E0["reported_pe"]) + 1e-6
+    assert abs(pe[True] - E1["reported_pe"]) <= 1e-8 * abs(E1["reported_pe"]) + 1e-6
