@@ -38,10 +38,14 @@ sys.path.insert(0, ROOT)
 
 DT_PS = 0.0005
 WORKLOADS = {
-    # name: (config number, description)
-    "c3": (3, "config3: 94,100-atom chain+water, 9.8 nm box, PME 100^3, rc 1.0 nm, skin 0.1 nm / 10 steps"),
+    # name: (config number, description); every system carries its 1-4 pairs
+    # as exceptions scaled 0.8333 (Coulomb) / 0.5 (LJ), 1-2 and 1-3 excluded
+    "c3": (3, "config3: 94,100-atom chain+water, 9.8 nm box, PME 100^3, rc 1.0 nm, skin 0.1 nm / 10 steps, "
+              "1-4 scaled 0.8333/0.5"),
     "c2": (2, "config2: 23,800-atom chain+water, 6.2 nm box, PME 64^3, rc 1.0 nm, skin 0.1 nm / 10 steps"),
     "c1": (1, "config1: 2,700-atom chain+water, 3.0 nm box, PME 32^3, rc 1.0 nm, skin 0.1 nm / 10 steps"),
+    "c4": (4, "config4: 32 independent lambda-window systems, 2,000-25,000 atoms each (log-uniform), "
+              "one context, PME ~0.1 nm grids"),
     "c5": (5, "config5: ~474,000-atom chain+water, 16.8 nm box, PME 180^3, rc 1.2 nm, tol 1e-5"),
 }
 # algorithmic FP32 flops per in-cutoff pair (FMA = 2): displacement 3,
@@ -179,8 +183,14 @@ def traffic_from_profiles(kernel, workload):
 
 
 def make_system(cfg):
+    """The named configuration with its 1-4 pairs as scaled exceptions
+    (Coulomb 0.8333, LJ 0.5, 1-2/1-3 excluded)."""
     from nexusmd_gb300 import synthetic as sy
-    return sy.config_system(cfg)
+    return sy.with_exceptions(sy.config_system(cfg))
+
+
+def oracle_desc(o, s):
+    return o.describe(s, box_mode=1, lb=[0.0, 0.0, 0.0], ub=list(s.box), exceptions=(s.exc_idx, s.exc_prm))
 
 
 def cpu_baseline(s, steps=2):
@@ -189,7 +199,7 @@ def cpu_baseline(s, steps=2):
     from oracle.nxo import Oracle, build
     build(ref=False)
     o = Oracle()
-    d = o.describe(s, box_mode=1, lb=[0.0, 0.0, 0.0], ub=list(s.box))
+    d = oracle_desc(o, s)
     t0 = time.perf_counter()
     phases = o.run_timed(d, s.pos, np.zeros_like(s.pos), DT_PS, steps)
     dt = time.perf_counter() - t0
@@ -207,16 +217,102 @@ def accuracy_check(s, eng_mixed):
     o = Oracle()
     box = o.box_explicit([0.0, 0.0, 0.0], list(s.box))
     eoff, el = o.exclusions(s.n, s.bonds)
-    F0, E0 = o.forces(o.describe(s, box_mode=1, lb=[0, 0, 0], ub=list(s.box)), s.pos, box, eoff, el)
+    eoff, el = o.union_exclusions(eoff, el, s.exc_idx)
+    F0, E0 = o.forces(oracle_desc(o, s), s.pos, box, eoff, el)
     eng_mixed.set_positions(s.pos)
     F = eng_mixed.compute_forces()
     err = float(np.sqrt(((F - F0) ** 2).sum() / (F0 ** 2).sum()))
     dmax = float(np.sqrt(((F - F0) ** 2).sum(1)).max())
     E = eng_mixed.energies()
     pe_rel = abs(E["potential"] - (E0["bond"] + E0["angle"] + E0["torsion"] + E0["recip"] + E0["self"]
-                                   + E0["coulomb"] + E0["vdw"] - E0["exclusion"]))
+                                   + E0["coulomb"] + E0["vdw"] - E0["exclusion"] + E0["exception"]))
     pe_ref = abs(E0["recip"]) + abs(E0["self"]) + abs(E0["coulomb"]) + abs(E0["vdw"])
     return {"force_rel_rms": err, "max_atom_force_err": dmax, "pe_rel_err": pe_rel / pe_ref}
+
+
+def nve_drift(s, v0, kw, steps=2000, every=20, equil=4000, rescale_every=100):
+    """Total-energy drift of the mixed engine without a thermostat: slope of
+    the least-squares line through KE + PE sampled every `every` steps,
+    in kJ/mol/ns per degree of freedom (3N).  The synthetic structure is not
+    relaxed, so `equil` steps with the velocities rescaled to 300 K every
+    `rescale_every` steps (on the host, outside the measurement) come first."""
+    import numpy as np
+    from nexusmd_gb300.engine import Engine
+    eng = Engine(s, precision=1, **kw)
+    eng.set_velocities(v0)
+    kT = 0.0083144626 * 300.0
+    for _ in range(equil // rescale_every):
+        eng.step(rescale_every, DT_PS)
+        _, v = eng.state()
+        ke = 0.5 * float((s.mass[:, None] * v * v).sum())
+        eng.set_velocities(v * np.sqrt(1.5 * s.n * kT / ke))
+    t, e = [], []
+    for k in range(steps // every):
+        eng.step(every, DT_PS)
+        E = eng.energies()
+        t.append((k + 1) * every * DT_PS)
+        e.append(E["kinetic"] + E["potential"])
+    eng.close()
+    t, e = np.array(t), np.array(e)
+    slope = float(np.polyfit(t, e, 1)[0])  # kJ/mol/ps
+    return {"value": slope * 1000.0 / (3 * s.n), "unit": "kJ/mol/ns/DOF", "steps": steps, "sample_every": every,
+            "precision": "mixed", "equilibration": "%d steps, velocities rescaled to 300 K every %d" % (equil, rescale_every),
+            "e_total_start": float(e[0]), "e_total_end": float(e[-1]), "e_total_std": float(e.std())}
+
+
+def batch_accuracy(systems, eng):
+    """Force rel-RMS of a (batched) mixed engine vs the FP64 oracle run per system."""
+    import numpy as np
+    from oracle.nxo import Oracle, build
+    build(ref=False)
+    o = Oracle()
+    F0 = []
+    pe_err = 0.0
+    F = eng.compute_forces()
+    E_eng = [eng.energies(k) for k in range(len(systems))]
+    for k, s in enumerate(systems):
+        box = o.box_explicit([0.0, 0.0, 0.0], list(s.box))
+        eoff, el = o.exclusions(s.n, s.bonds)
+        eoff, el = o.union_exclusions(eoff, el, s.exc_idx)
+        f, E0 = o.forces(oracle_desc(o, s), s.pos, box, eoff, el)
+        F0.append(f)
+        pe0 = (E0["bond"] + E0["angle"] + E0["torsion"] + E0["recip"] + E0["self"] + E0["coulomb"] + E0["vdw"]
+               - E0["exclusion"] + E0["exception"])
+        scale = abs(E0["recip"]) + abs(E0["self"]) + abs(E0["coulomb"]) + abs(E0["vdw"])
+        pe_err = max(pe_err, abs(E_eng[k]["potential"] - pe0) / scale)
+    F0 = np.concatenate(F0)
+    err = float(np.sqrt(((F - F0) ** 2).sum() / (F0 ** 2).sum()))
+    dmax = float(np.sqrt(((F - F0) ** 2).sum(1)).max())
+    return {"force_rel_rms": err, "max_atom_force_err": dmax, "pe_rel_err_max_over_systems": pe_err}
+
+
+def other_workload(cfg, steps, warmup, device, check=True):
+    """Throughput (and accuracy) of another named configuration: 4 = the
+    32-system uneven lambda-window batch in one context, 5 = ~474k atoms."""
+    import numpy as np
+    from nexusmd_gb300 import synthetic as sy
+    from nexusmd_gb300.engine import Engine
+    if cfg == 4:
+        systems = [sy.with_exceptions(x) for x in sy.batch_systems()]
+    else:
+        systems = [make_system(cfg)]
+    n = sum(x.n for x in systems)
+    v0 = np.concatenate([sy.maxwell_boltzmann(x.mass, 300.0, seed=1000 + cfg + k) for k, x in enumerate(systems)])
+    eng = Engine(systems, precision=1, skin=0.1, rebuild_interval=10, box="explicit", device=device,
+                 exceptions=True)
+    eng.set_velocities(v0)
+    eng.step(warmup, DT_PS)
+    rb0 = eng.rebuilds()
+    ms = eng.time_steps(steps, DT_PS)
+    out = {"workload": WORKLOADS["c%d" % cfg][1], "systems": len(systems), "atoms": n,
+           "value": n * steps / (ms * 1e-3), "unit": "atom-steps/s", "ms_per_step": ms / steps,
+           "ns_per_day": (1.0 / (ms / steps * 1e-3)) * DT_PS * 1e-3 * 86400.0, "steps": steps,
+           "list_rebuilds": eng.rebuilds() - rb0, "precision": "mixed"}
+    if check:
+        eng.set_positions(np.concatenate([x.pos for x in systems]))
+        out["accuracy_vs_fp64_oracle"] = batch_accuracy(systems, eng)
+    eng.close()
+    return out
 
 
 def native(args):
@@ -229,7 +325,7 @@ def native(args):
     load_library()
     from nexusmd_gb300 import synthetic as sy
     v0 = sy.maxwell_boltzmann(s.mass, 300.0, seed=1000 + cfg)
-    kw = dict(skin=0.1, rebuild_interval=10, box="explicit", device=local)
+    kw = dict(skin=0.1, rebuild_interval=10, box="explicit", device=local, exceptions=True)
     eng = Engine(s, precision=1, **kw)
     eng.set_velocities(v0)
     eng.step(args.warmup, DT_PS)
@@ -314,6 +410,12 @@ def native(args):
                              "mixed_over_fp64": value / v64}
         if not args.no_check:
             out["accuracy_vs_fp64_oracle"] = accuracy_check(s, eng)
+        del eng
+        if not args.quick:
+            out["nve_drift"] = nve_drift(s, v0, kw)
+            out["other_workloads"] = {
+                "c4": other_workload(4, 200, 10, local, check=not args.no_check),
+                "c5": other_workload(5, 100, 5, local, check=not args.no_check)}
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_baseline(s, steps=args.cpu_steps)
     if rank == 0:
@@ -327,7 +429,7 @@ def _oracle_worker(cfg, steps, q):
     from oracle.nxo import Oracle
     s = make_system(cfg)
     o = Oracle()
-    d = o.describe(s, box_mode=1, lb=[0.0, 0.0, 0.0], ub=list(s.box))
+    d = oracle_desc(o, s)
     t0 = time.perf_counter()
     o.run_timed(d, s.pos, np.zeros_like(s.pos), DT_PS, steps)
     q.put((s.n, time.perf_counter() - t0))
@@ -379,11 +481,13 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=50)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
-    ap.add_argument("--workload", default="c3", choices=sorted(WORKLOADS))
+    # single-system workloads; the 32-system batch is reported under other_workloads
+    ap.add_argument("--workload", default="c3", choices=sorted(k for k in WORKLOADS if k != "c4"))
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--ref-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-check", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="skip NVE drift and the other workloads")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -230,6 +230,38 @@ def test_exceptions_physics_mode(oracle, depth):
         eng.close()
 
 
+def test_batched_uneven_systems_match_per_system_oracle(oracle):
+    """Several independent systems of uneven size (lambda-scaled chain
+    charges, own boxes and PME grids) in one context: each system's forces,
+    energies and pair set equal the oracle's for that system alone."""
+    systems = [sy.with_exceptions(x) for x in sy.batch_systems(count=4, seed=77, lo=2000, hi=6000)]
+    sizes = [x.n for x in systems]
+    assert len(set(sizes)) == len(sizes)
+    for prec, tol in ((0, 1e-9), (1, 1e-5)):
+        eng = _engine(systems, precision=prec, skin=0.1, rebuild_interval=10, box="explicit", exceptions=True)
+        F = eng.compute_forces()
+        off = 0
+        for k, s in enumerate(systems):
+            lb, ub = np.zeros(3), s.box.copy()
+            box = oracle.box_explicit(lb, ub)
+            eo, el = oracle.exclusions(s.n, s.bonds)
+            eo, el = oracle.union_exclusions(eo, el, s.exc_idx)
+            d = oracle.describe(s, box_mode=1, lb=lb, ub=ub, exceptions=(s.exc_idx, s.exc_prm))
+            F0, E0 = oracle.forces(d, s.pos, box, eo, el)
+            assert rel_rms(F[off:off + s.n], F0) <= tol, (prec, k, rel_rms(F[off:off + s.n], F0))
+            E = eng.energies(k)
+            scale = max(abs(E0[t]) for t in TERMS)
+            etol = 1e-9 if prec == 0 else 2e-5
+            for t in TERMS + ("exception",):
+                assert abs(E[t] - E0[t]) <= etol * scale + 1e-6, (prec, k, t, E[t], E0[t])
+            if prec == 1:
+                ref = oracle.neighbor_pairs(s.pos, box, eo, el, s.cutoff)
+                ref = ref[np.lexsort((ref[:, 1], ref[:, 0]))]
+                assert np.array_equal(eng.pairs(k), ref)
+            off += s.n
+        eng.close()
+
+
 def test_exceptions_bit_reproducible():
     s = sy.with_exceptions(sy.config_system(1))
     outs = []
