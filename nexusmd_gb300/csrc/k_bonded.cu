@@ -37,6 +37,12 @@ __device__ __forceinline__ V3<R> scale(const V3<R> &a, R s) {
 // minimumImageVector(p[a], p[b]) = p[a] - p[b], one shift per component
 template <typename R>
 __device__ __forceinline__ V3<R> disp(const DevView &v, const SysDev &S, int a, int b) {
+    if (sizeof(R) == 4) {
+        // FP64 difference, shift decided in FP32 (min_image_f)
+        return mk<R>((R)min_image_f(v.x[a] - v.x[b], S.L[0], S.halfLf[0]),
+                     (R)min_image_f(v.y[a] - v.y[b], S.L[1], S.halfLf[1]),
+                     (R)min_image_f(v.z[a] - v.z[b], S.L[2], S.halfLf[2]));
+    }
     double dx = min_image(v.x[a] - v.x[b], S.L[0], S.halfL[0]);
     double dy = min_image(v.y[a] - v.y[b], S.L[1], S.halfL[1]);
     double dz = min_image(v.z[a] - v.z[b], S.L[2], S.halfL[2]);

@@ -67,25 +67,33 @@ __global__ void __launch_bounds__(256) k_integrate(DevView v, double dt, int rep
             v.vz[s] = u[2];
         }
         if (v.mixed) {
-            int c3 = v.cell3[s];
-            int ci[3] = {c3 & 1023, (c3 >> 10) & 1023, (c3 >> 20) & 1023};
-            float o[3];
-#pragma unroll
-            for (int c = 0; c < 3; ++c)
-                o[c] = (float)min_image(p[c] - (S.lb[c] + ci[c] * S.cs[c]), S.L[c], S.halfL[c]);
-            float4 pf = v.pf[s];
-            v.pf[s] = make_float4(o[0], o[1], o[2], pf.w);
-        }
-        if (v.skin_half2 > 0.0) {
-            double d2 = 0.0;
+            // One FP64 subtraction per component serves both the FP32 cell
+            // offset (offset at the last rebuild + displacement since) and
+            // the skin check; shifts and squares in FP32, which keeps this
+            // kernel off the slow FP64 pipe except for the update itself.
+            float4 r = v.oref[s];
+            float d[3], d2 = 0.0f;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                double d = min_image(p[c] - v.xref[(size_t)c * v.N + s], S.L[c], S.halfL[c]);
-                d2 += d * d;
+                d[c] = min_image_f(p[c] - v.xref[(size_t)c * v.N + s], S.L[c], S.halfLf[c]);
+                d2 = fmaf(d[c], d[c], d2);
             }
-            if (d2 > v.skin_half2) atomicOr(&v.flags->skin_hit, 1);
+            v.pf[s] = make_float4(r.x + d[0], r.y + d[1], r.z + d[2], r.w);
+            // a hair under skin/2: FP32 rounding can only trigger a rebuild early
+            if (v.skin_half2 > 0.0 && d2 > (float)v.skin_half2 * 0.99999f) atomicOr(&v.flags->skin_hit, 1);
+        } else {
+            if (v.skin_half2 > 0.0) {
+                double d2 = 0.0;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    double d = min_image(p[c] - v.xref[(size_t)c * v.N + s], S.L[c], S.halfL[c]);
+                    d2 += d * d;
+                }
+                if (d2 > v.skin_half2) atomicOr(&v.flags->skin_hit, 1);
+            }
+            // FP64 accumulators can hold a non-finite sum; int64 ones cannot
+            if (!(isfinite(F[0]) && isfinite(F[1]) && isfinite(F[2]))) atomicOr(&v.flags->error, ERR_NONFINITE);
         }
-        if (!(isfinite(F[0]) && isfinite(F[1]) && isfinite(F[2]))) atomicOr(&v.flags->error, ERR_NONFINITE);
     }
     if (report) energy_add(v.E, sys, E_KIN, ke);
 }

@@ -163,6 +163,7 @@ __global__ void k_derive(DevView v, int gated) {
             o[d] = (float)min_image(p[d] - org, S.L[d], S.halfL[d]);
         }
         v.pf[s] = make_float4(o[0], o[1], o[2], (float)qs);
+        v.oref[s] = make_float4(o[0], o[1], o[2], (float)qs);
         v.ljf[s] = make_float2((float)sg, (float)ep);
     } else {
         v.qs[s] = qs;

@@ -23,11 +23,10 @@ __global__ void __launch_bounds__(256) k_exclusions(DevView v, int energy) {
         int ii = p.x, jj = p.y;
         sys = v.sys_of[ii];
         const SysDev &S = v.sys[sys];
-        double dx = min_image(v.x[ii] - v.x[jj], S.L[0], S.halfL[0]);
-        double dy = min_image(v.y[ii] - v.y[jj], S.L[1], S.halfL[1]);
-        double dz = min_image(v.z[ii] - v.z[jj], S.L[2], S.halfL[2]);
         if (MIXED) {
-            float fdx = (float)dx, fdy = (float)dy, fdz = (float)dz;
+            float fdx = min_image_f(v.x[ii] - v.x[jj], S.L[0], S.halfLf[0]);
+            float fdy = min_image_f(v.y[ii] - v.y[jj], S.L[1], S.halfLf[1]);
+            float fdz = min_image_f(v.z[ii] - v.z[jj], S.L[2], S.halfLf[2]);
             float r = sqrtf(fdx * fdx + fdy * fdy + fdz * fdz);
             float rinv = 1.0f / r;
             float xa = S.alphaf * r;
@@ -47,6 +46,9 @@ __global__ void __launch_bounds__(256) k_exclusions(DevView v, int energy) {
                 e = (double)S.alphaf * kTwoOverSqrtPi * (double)qq;
             }
         } else {
+            double dx = min_image(v.x[ii] - v.x[jj], S.L[0], S.halfL[0]);
+            double dy = min_image(v.y[ii] - v.y[jj], S.L[1], S.halfL[1]);
+            double dz = min_image(v.z[ii] - v.z[jj], S.L[2], S.halfL[2]);
             double r = sqrt(dx * dx + dy * dy + dz * dz);
             double rinv = 1.0 / r;
             double xa = S.alpha * r;
@@ -88,15 +90,15 @@ __global__ void __launch_bounds__(256) k_exceptions(DevView v, int energy) {
         sys = v.sys_of[ii];
         const SysDev &S = v.sys[sys];
         double4 prm = v.xc_prm[t];
-        double dx = min_image(v.x[ii] - v.x[jj], S.L[0], S.halfL[0]);
-        double dy = min_image(v.y[ii] - v.y[jj], S.L[1], S.halfL[1]);
-        double dz = min_image(v.z[ii] - v.z[jj], S.L[2], S.halfL[2]);
         if (MIXED) {
-            float fdx = (float)dx, fdy = (float)dy, fdz = (float)dz;
+            float fdx = min_image_f(v.x[ii] - v.x[jj], S.L[0], S.halfLf[0]);
+            float fdy = min_image_f(v.y[ii] - v.y[jj], S.L[1], S.halfLf[1]);
+            float fdz = min_image_f(v.z[ii] - v.z[jj], S.L[2], S.halfLf[2]);
             float rinv2 = 1.0f / (fdx * fdx + fdy * fdy + fdz * fdz);
             float rinv = sqrtf(rinv2);
             float coul = (float)prm.x * rinv;
-            float s2 = (float)(prm.y * prm.y) * rinv2;
+            float sg = (float)prm.y;
+            float s2 = sg * sg * rinv2;
             float s6 = s2 * s2 * s2;
             float e4 = (float)prm.z;
             float dEdR = (coul + e4 * (12.0f * s6 - 6.0f) * s6) * rinv2;
@@ -108,6 +110,9 @@ __global__ void __launch_bounds__(256) k_exceptions(DevView v, int energy) {
             acc_add(static_cast<long long *>(v.fz) + jj, -fdz * dEdR);
             e = (double)coul + (double)(e4 * (s6 - 1.0f) * s6);
         } else {
+            double dx = min_image(v.x[ii] - v.x[jj], S.L[0], S.halfL[0]);
+            double dy = min_image(v.y[ii] - v.y[jj], S.L[1], S.halfL[1]);
+            double dz = min_image(v.z[ii] - v.z[jj], S.L[2], S.halfL[2]);
             double r2 = dx * dx + dy * dy + dz * dz;
             double rinv = 1.0 / sqrt(r2);
             double coul = prm.x * rinv;

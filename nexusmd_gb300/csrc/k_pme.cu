@@ -42,8 +42,7 @@ __device__ __forceinline__ void bspline5(R dr, R *th, R *dth) {
 }
 
 __device__ __forceinline__ void grid_add(long long *g, float v) {
-    atomicAdd(reinterpret_cast<unsigned long long *>(g),
-              static_cast<unsigned long long>(__float2ll_rn(v * 4294967296.0f)));
+    atomicAdd(reinterpret_cast<unsigned long long *>(g), to_fixed32(v));
 }
 __device__ __forceinline__ void grid_add(double *g, double v) { atomicAdd(g, v); }
 
@@ -80,10 +79,12 @@ __global__ void __launch_bounds__(128) k_spread(DevView v, const FftSysDev *fs) 
     R q = (R)v.q[s];
     Acc *g = static_cast<Acc *>(v.grid_acc) + F.roff;
     int K1 = F.K[1], K2 = F.K[2];
+#pragma unroll
     for (int ix = 0; ix < 5; ++ix) {
         int xi = idx[0] + ix;
         xi -= xi >= F.K[0] ? F.K[0] : 0;
         R qx = q * th[0][ix];
+#pragma unroll
         for (int iy = 0; iy < 5; ++iy) {
             int yi = idx[1] + iy;
             yi -= yi >= K1 ? K1 : 0;
@@ -127,9 +128,11 @@ __global__ void __launch_bounds__(128) k_gather(DevView v, const FftSysDev *fs) 
     const R *g = static_cast<const R *>(v.grid_real) + F.roff;
     int K1 = F.K[1], K2 = F.K[2];
     R fx = 0, fy = 0, fz = 0;
+#pragma unroll
     for (int ix = 0; ix < 5; ++ix) {
         int xi = id.x + ix;
         xi -= xi >= F.K[0] ? F.K[0] : 0;
+#pragma unroll
         for (int iy = 0; iy < 5; ++iy) {
             int yi = id.y + iy;
             yi -= yi >= K1 ? K1 : 0;

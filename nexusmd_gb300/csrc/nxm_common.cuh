@@ -96,9 +96,22 @@ __device__ __forceinline__ void atomic_add_fixed(long long *a, double v, double 
               static_cast<unsigned long long>(__double2ll_rn(v * scale)));
 }
 
+// float -> int64 fixed point in units of 2^-32, without the FP64 pipe (on
+// this GPU double-precision and 64-bit conversion instructions issue far
+// slower than FP32 and int32 ones): v = h + l with h = rint(v) and
+// l = v - h in [-1/2, 1/2], both exact in FP32; h converts to int32 as is
+// and l at 2^-31, so the result is round(v * 2^31) * 2 -- the 2^-32 grid
+// less its last bit, for |v| < 2^31.
+__device__ __forceinline__ unsigned long long to_fixed32(float v) {
+    float h = rintf(v);
+    float l = v - h;
+    long long hi = __float2int_rn(h);
+    long long lo = __float2int_rn(l * 2147483648.0f);
+    return (static_cast<unsigned long long>(hi) << 32) + (static_cast<unsigned long long>(lo) << 1);
+}
+
 __device__ __forceinline__ void acc_add(long long *a, float v) {
-    atomicAdd(reinterpret_cast<unsigned long long *>(a),
-              static_cast<unsigned long long>(__double2ll_rn((double)v * kForceScale)));
+    atomicAdd(reinterpret_cast<unsigned long long *>(a), to_fixed32(v));
 }
 __device__ __forceinline__ void acc_add(double *a, double v) { atomicAdd(a, v); }
 
@@ -113,6 +126,20 @@ __device__ __forceinline__ double min_image(double d, double L, double halfL) {
     else if (d < -halfL)
         d += L;
     return d;
+}
+
+// The same single-shift minimum image for the mixed-precision paths: the FP64
+// difference d is rounded to FP32 once and the shift is decided on that
+// float (it can differ from the FP64 decision only for |d| within FP32
+// rounding of L/2, which bonded and excluded pairs never approach); a
+// shifted component is re-formed in FP64 before its rounding.
+__device__ __forceinline__ float min_image_f(double d, double L, float halfLf) {
+    float f = (float)d;
+    if (f > halfLf)
+        f = (float)(d - L);
+    else if (f < -halfLf)
+        f = (float)(d + L);
+    return f;
 }
 
 template <typename T>

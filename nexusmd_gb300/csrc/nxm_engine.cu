@@ -406,6 +406,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     v_.ncount = dalloc<int>(N_);
     v_.dtab = dalloc<float4>((size_t)S * kDtabStride);
     v_.xref = dalloc<double>(3 * (size_t)N_);
+    v_.oref = dalloc<float4>(N_);
     v_.tmp = dalloc<double>(11 * (size_t)N_);
     if (!v_.nl16 || !v_.tmp) return "device allocation failed (neighbour list)";
 

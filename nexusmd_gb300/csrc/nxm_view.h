@@ -47,6 +47,7 @@ struct DevView {
     int hood_cap;        // capacity of a staged neighbourhood (atoms)
     float4 *dtab;        // [S][kDtabStride] cell-image displacement per code
     double *xref;        // [3][N] positions at the last rebuild
+    float4 *oref;        // mixed: cell offsets at the last rebuild, .w = q * sqrt(ke)
     int *excl_off, *excl_lst;  // CSR by original index, partners as original indices
     // scratch used by the permutation
     double *tmp;         // [11][N]
