@@ -165,6 +165,9 @@ Engine::~Engine() {
     fft_plan_free(plan_);
     if (h_E_) cudaFreeHost(h_E_);
     if (h_flags_) cudaFreeHost(h_flags_);
+    if (ev_fork_) cudaEventDestroy(ev_fork_);
+    if (ev_join_) cudaEventDestroy(ev_join_);
+    if (st_pme_) cudaStreamDestroy(st_pme_);
     if (st_) cudaStreamDestroy(st_);
 }
 
@@ -345,6 +348,10 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
 
     // ---- device memory
     cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking);
+    // second stream and fork/join events: the PME branch of the step graph
+    cudaStreamCreateWithFlags(&st_pme_, cudaStreamNonBlocking);
+    cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming);
     v_ = DevView{};
     v_.N = N_;
     v_.S = S;
@@ -723,13 +730,24 @@ static int force_launch_count(const DevView &v) {
     return n;
 }
 
-static int force_launches(const DevView &v, const FftPlan &plan, int energy, cudaStream_t st) {
+// All force kernels.  With a second stream `pme_st`, the PME chain (spread,
+// FFT, gather) runs there as an independent branch: it shares nothing with
+// the bonded / pair / exclusion kernels but the force words, which both add
+// to with integer atomics (order-free); the caller joins the streams before
+// the update.
+static int force_launches(const DevView &v, const FftPlan &plan, int energy, cudaStream_t st,
+                          cudaStream_t pme_st = nullptr) {
     int n = 0;
+    bool nb = (v.force_mask & NXM_FORCE_NONBONDED) != 0;
+    if (nb && pme_st) {
+        launch_pme(v, plan, energy, pme_st);
+        n += 7;
+    }
     if (v.nb + v.na + v.nt) {
         launch_bonded(v, energy, st);
         ++n;
     }
-    if (v.force_mask & NXM_FORCE_NONBONDED) {
+    if (nb) {
         launch_pairs(v, energy, st);
         ++n;
         if (v.nex) {
@@ -740,8 +758,10 @@ static int force_launches(const DevView &v, const FftPlan &plan, int energy, cud
             launch_exceptions(v, energy, st);
             ++n;
         }
-        launch_pme(v, plan, energy, st);
-        n += 7;
+        if (!pme_st) {
+            launch_pme(v, plan, energy, st);
+            n += 7;
+        }
     }
     return n;
 }
@@ -805,7 +825,12 @@ std::string Engine::build_graph(double dt, int report) {
     // tail: forces and update, after the conditional node
     e = cudaStreamBeginCaptureToGraph(st_, g, &cnode, nullptr, 1, mode);
     if (e != cudaSuccess) return fail_capture("capture tail", e);
-    force_launches(v_, plan_, report, st_);
+    // PME as a parallel branch on the second stream, joined before the update
+    cudaEventRecord(ev_fork_, st_);
+    cudaStreamWaitEvent(st_pme_, ev_fork_, 0);
+    force_launches(v_, plan_, report, st_, st_pme_);
+    cudaEventRecord(ev_join_, st_pme_);
+    cudaStreamWaitEvent(st_, ev_join_, 0);
     launch_integrate(v_, dt, report, st_);
     e = cudaStreamEndCapture(st_, &captured);
     if (e != cudaSuccess) return fail_capture("end tail", e);

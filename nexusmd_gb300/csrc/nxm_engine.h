@@ -101,6 +101,8 @@ private:
     std::vector<SysDev> sysd_;
     std::vector<SysHost> sysh_;
     cudaStream_t st_ = nullptr;
+    cudaStream_t st_pme_ = nullptr;  // PME branch of the step graph (captured only)
+    cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
     int N_ = 0;
     int mixed_ = 1;
     int interval_ = 1;
