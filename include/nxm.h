@@ -93,6 +93,9 @@ typedef struct {
     int32_t max_neighbors;    /* list capacity per atom; 0 = from density */
     int32_t exceptions;       /* Simulate only: 1 = apply the system XML's <Exceptions>
                                  (OpenMM semantics); 0 = ignore them, as the reference */
+    int32_t autotune;         /* 1 (default): at creation, time candidate launch shapes that
+                                 change no result (FFT blocking, spread/gather block size)
+                                 and keep the fastest; see nxm_get_tuning */
 } nxm_options;
 
 /* Energies of one system (kJ/mol) at the last evaluation that computed them. */
@@ -166,6 +169,11 @@ int nxm_profile_phases(nxm_ctx *ctx, int32_t nsteps, double dt, double *ms, int3
  * via NonbondedForce.cpp:474-500); this engine rebuilds when the device
  * decides (list age or displacement beyond half the skin). */
 int nxm_rebuild_count(nxm_ctx *ctx, int64_t *count);
+
+/* Launch shapes in use: [0] FFT real lines per z-pass block, [1] FFT
+ * columns per y/x-pass block, [2] threads per spread/gather block (the
+ * autotuner's picks, or the defaults 16, 8, 128). */
+int nxm_get_tuning(nxm_ctx *ctx, int32_t out[3]);
 
 /* Kernel launches one step issues (steady state, no list rebuild). */
 int nxm_launches_per_step(nxm_ctx *ctx, int32_t *launches, int32_t *rebuild_launches);

@@ -26,7 +26,8 @@ from .engine import load_library
 
 class _Opts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("skin", C.c_double), ("rebuild_interval", C.c_int32),
-                ("device", C.c_int32), ("max_neighbors", C.c_int32), ("exceptions", C.c_int32)]
+                ("device", C.c_int32), ("max_neighbors", C.c_int32), ("exceptions", C.c_int32),
+                ("autotune", C.c_int32)]
 
 
 def _lib():
@@ -265,12 +266,13 @@ class TaskDispatcher:
         self._L.nxm_dispatcher_enable_nonbonded_force(self._h)
 
     def SetOptions(self, precision="mixed", skin=0.1, rebuild_interval=10, device=0, max_neighbors=0,
-                   exceptions=False):
+                   exceptions=False, autotune=True):
         """Engine settings the reference hard-codes (precision "mixed" or "fp64").
         exceptions=True applies the system XML's <Exceptions> (scaled 1-4 pairs,
-        OpenMM semantics), which the reference parses but ignores."""
+        OpenMM semantics), which the reference parses but ignores; autotune
+        times result-neutral launch shapes at set-up and keeps the fastest."""
         o = _Opts(PRECISIONS[precision], float(skin), int(rebuild_interval), int(device), int(max_neighbors),
-                  1 if exceptions else 0)
+                  1 if exceptions else 0, 1 if autotune else 0)
         _err(self._L, self._L.nxm_dispatcher_set_options(self._h, C.byref(o)), "SetOptions")
 
     def Simulate(self, systemFilename, stateFilename, inputFilename, outputFilename, StepSize, TotalSteps,

@@ -10,6 +10,8 @@
 // convolution with the influence function and the reciprocal energy sum
 // (NonbondedForce.cpp:323-388) are fused into the x pass between its forward
 // and inverse transforms, so the spectrum never makes an extra trip to memory.
+#include <mutex>
+
 #include "nxm_fft.h"
 #include "nxm_view.h"
 
@@ -358,17 +360,29 @@ void fft_plan_build(FftPlan &p, int mixed) {
     cudaMemcpy(p.zwork, z.data(), sizeof(FftWork) * p.nz, cudaMemcpyHostToDevice);
     cudaMemcpy(p.ywork, y.data(), sizeof(FftWork) * p.ny, cudaMemcpyHostToDevice);
     cudaMemcpy(p.xwork, x.data(), sizeof(FftWork) * p.nx, cudaMemcpyHostToDevice);
-    size_t big = p.smem_z > p.smem_y ? p.smem_z : p.smem_y;
+    // The dynamic shared-memory limit is a per-kernel attribute shared by
+    // every context (and plan) of the process on a device: only ever raise
+    // it, so a plan with smaller lines cannot lower it under another one.
+    static std::mutex mu;
+    static int seen[2][kMaxSmemDevices] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= kMaxSmemDevices) dev = 0;
+    int big = (int)(p.smem_z > p.smem_y ? p.smem_z : p.smem_y);
+    std::lock_guard<std::mutex> lock(mu);
+    // launches up to 48 KB need no attribute
+    if (big <= 48 * 1024 || big <= seen[mixed ? 1 : 0][dev]) return;
+    seen[mixed ? 1 : 0][dev] = big;
     if (mixed) {
-        cudaFuncSetAttribute(k_fft_z_fwd<float2, long long>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)big);
-        cudaFuncSetAttribute(k_fft_y<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)big);
-        cudaFuncSetAttribute(k_fft_x_conv<float2, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)big);
-        cudaFuncSetAttribute(k_fft_z_inv<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)big);
+        cudaFuncSetAttribute(k_fft_z_fwd<float2, long long>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+        cudaFuncSetAttribute(k_fft_y<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+        cudaFuncSetAttribute(k_fft_x_conv<float2, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+        cudaFuncSetAttribute(k_fft_z_inv<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     } else {
-        cudaFuncSetAttribute(k_fft_z_fwd<double2, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)big);
-        cudaFuncSetAttribute(k_fft_y<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)big);
-        cudaFuncSetAttribute(k_fft_x_conv<double2, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)big);
-        cudaFuncSetAttribute(k_fft_z_inv<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)big);
+        cudaFuncSetAttribute(k_fft_z_fwd<double2, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+        cudaFuncSetAttribute(k_fft_y<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+        cudaFuncSetAttribute(k_fft_x_conv<double2, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+        cudaFuncSetAttribute(k_fft_z_inv<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     }
 }
 

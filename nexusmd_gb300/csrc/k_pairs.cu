@@ -14,6 +14,8 @@
 // r^2 < cutoff^2.  The list holds a superset (cutoff + skin, FP32 test with
 // a safety margin); in mixed mode the FP32 r^2 settles every pair except
 // those within 1e-5 relative of the cutoff, which are re-tested in FP64.
+#include <mutex>
+
 #include "nxm_hood.cuh"
 #include "nxm_view.h"
 
@@ -523,13 +525,29 @@ static size_t smem_pairs(int cap, int mixed) {
     return mixed ? (size_t)cap * (sizeof(float4) + sizeof(float2)) + tail_bytes() : tail_bytes();
 }
 
+// The dynamic shared-memory limit is a per-kernel attribute shared by every
+// context of the process on a device: it is only ever raised, so a context
+// with a smaller neighbourhood cannot lower it under another one.
 void tiles_set_smem(int cap) {
+    static std::mutex mu;
+    static int seen_build[kMaxSmemDevices] = {}, seen_pairs[kMaxSmemDevices] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= kMaxSmemDevices) dev = 0;
     int b = (int)smem_build(cap), m = (int)smem_pairs(cap, 1);
-    cudaFuncSetAttribute(k_build, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-    cudaFuncSetAttribute(k_pairs_mixed<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-    cudaFuncSetAttribute(k_pairs_mixed<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-    cudaFuncSetAttribute(k_pairs_mixed<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-    cudaFuncSetAttribute(k_pairs_mixed<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    std::lock_guard<std::mutex> lock(mu);
+    // launches up to 48 KB need no attribute
+    if (b > 48 * 1024 && b > seen_build[dev]) {
+        cudaFuncSetAttribute(k_build, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+        seen_build[dev] = b;
+    }
+    if (m > 48 * 1024 && m > seen_pairs[dev]) {
+        cudaFuncSetAttribute(k_pairs_mixed<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+        cudaFuncSetAttribute(k_pairs_mixed<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+        cudaFuncSetAttribute(k_pairs_mixed<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+        cudaFuncSetAttribute(k_pairs_mixed<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+        seen_pairs[dev] = m;
+    }
 }
 
 void launch_build(const DevView &v, cudaStream_t st) {

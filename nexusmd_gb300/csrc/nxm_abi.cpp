@@ -35,6 +35,8 @@ void nxm_default_options(nxm_options *opt) {
     opt->rebuild_interval = 10;
     opt->device = 0;
     opt->max_neighbors = 0;
+    opt->exceptions = 0;
+    opt->autotune = 1;
 }
 
 static int code_for(const std::string &e) {
@@ -214,6 +216,13 @@ int nxm_time_steps(nxm_ctx *ctx, int32_t nsteps, double dt, double *ms) {
 int nxm_profile_phases(nxm_ctx *ctx, int32_t nsteps, double dt, double *ms, int32_t cap) {
     if (!ctx || !ms || nsteps <= 0 || cap < nxm::kProfilePhases) return fail(NXM_ERR_INVALID, "bad argument");
     NXM_CALL(ctx->eng.profile(nsteps, dt, ms));
+}
+
+int nxm_get_tuning(nxm_ctx *ctx, int32_t out[3]) {
+    if (!ctx || !out) return fail(NXM_ERR_INVALID, "null argument");
+    const int *t = ctx->eng.tuning();
+    for (int k = 0; k < 3; ++k) out[k] = t[k];
+    return NXM_OK;
 }
 
 int nxm_rebuild_count(nxm_ctx *ctx, int64_t *count) {

@@ -636,24 +636,8 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         // FFT work lists only for systems with nonbonded forces: systems
         // without them keep an empty grid that no block touches
         fft_plan_build(plan_, mixed_);
-        // shared-memory sub-grid of the grouped spread: a group's cells plus
-        // the drift margin on both sides plus the stencil reach, per axis
-        v_.spread_margin = 0.5 * skin + 1e-3;
-        int sp_cap = 0;
-        for (int s = 0; s < S; ++s) {
-            const SysDev &D = sysd_[s];
-            int ncell[3] = {1, 1, group_g[s]};
-            long long vol = 1;
-            for (int d = 0; d < 3; ++d) {
-                double span = ncell[d] * D.cs[d] + 2 * v_.spread_margin;
-                int e = (int)std::ceil(span / D.L[d] * D.K[d]) + 1 + kOrder;
-                vol *= std::min(e, D.K[d]);
-            }
-            sp_cap = (int)std::max<long long>(sp_cap, vol);
-        }
-        v_.spread_cap = std::min(sp_cap, 12 * 1024);  // <= 96 KB; larger groups take the global path
-        spread_set_smem(v_.spread_cap);
     }
+    v_.pme_block = 128;
     // systems without nonbonded forces: zero their charges in the PME and
     // pair paths by skipping them entirely (no list, no grid)
     v_.E = dalloc<long long>((size_t)S * E_SLOTS);
@@ -681,7 +665,80 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     std::string e = check("set-up");
     if (!e.empty()) return e;
     cudaStreamSynchronize(st_);
-    return check("set-up");
+    e = check("set-up");
+    if (!e.empty()) return e;
+    if (opt.autotune && (v_.force_mask & NXM_FORCE_NONBONDED) && plan_.nz) return autotune();
+    return "";
+}
+
+// Launch shapes that change no result, chosen by timing each candidate on
+// this context's own buffers (grid contents do not matter for the timing;
+// what the timed kernels accumulate is cleared afterwards):
+//  * FFT: real lines per z-pass block x columns per y/x-pass block -- every
+//    line is transformed by the same arithmetic whatever the blocking;
+//  * spread / gather: threads per block -- the sums are integer atomics.
+// The neighbour-list cell groups are not tuned: their size changes the
+// summation order of the pair forces, and a choice that followed timing
+// noise would break run-to-run bit reproducibility.
+std::string Engine::autotune() {
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    auto time3 = [&](auto &&launch) {
+        launch();  // warm-up
+        cudaEventRecord(a, st_);
+        for (int r = 0; r < 3; ++r) launch();
+        cudaEventRecord(b, st_);
+        cudaEventSynchronize(b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        return ms;
+    };
+    float best = 1e30f;
+    int bz = plan_.zlines, bc = plan_.cols;
+    for (int zl : {8, 16, 32})
+        for (int cols : {4, 8, 16}) {
+            fft_plan_free(plan_);
+            plan_.zlines = zl;
+            plan_.cols = cols;
+            fft_plan_build(plan_, mixed_);
+            float t = time3([&] { launch_fft_convolve(v_, plan_, 0, st_); });
+            if (t < best) {
+                best = t;
+                bz = zl;
+                bc = cols;
+            }
+        }
+    fft_plan_free(plan_);
+    plan_.zlines = bz;
+    plan_.cols = bc;
+    fft_plan_build(plan_, mixed_);
+    best = 1e30f;
+    int bt = v_.pme_block;
+    for (int t : {64, 128, 256}) {
+        v_.pme_block = t;
+        float ms = time3([&] {
+            launch_spread(v_, plan_, st_);
+            launch_gather(v_, plan_, st_);
+        });
+        if (ms < best) {
+            best = ms;
+            bt = t;
+        }
+    }
+    v_.pme_block = bt;
+    // the gather added into the force words
+    size_t fb = sizeof(long long) * (size_t)N_;
+    cudaMemsetAsync(v_.fx, 0, fb, st_);
+    cudaMemsetAsync(v_.fy, 0, fb, st_);
+    cudaMemsetAsync(v_.fz, 0, fb, st_);
+    cudaStreamSynchronize(st_);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    tune_[0] = bz;
+    tune_[1] = bc;
+    tune_[2] = bt;
+    return check("autotune");
 }
 
 std::string Engine::set_positions(const double *xyz) {

@@ -74,6 +74,7 @@ public:
     const SysHost &sys(int s) const { return sysh_[s]; }
     int launches_per_step() const { return launches_per_step_; }
     int launches_per_rebuild() const { return launches_per_rebuild_; }
+    const int *tuning() const { return tune_; }
     // neighbour-list rebuilds since creation, as of the last finished call
     long long rebuild_count() const { return h_flags_ ? reinterpret_cast<const Flags *>(h_flags_)->nrebuild : 0; }
 
@@ -89,6 +90,10 @@ private:
         bool ok = false;
     };
     StepGraph graph_[2];
+    // Launch shapes tuned at set-up: FFT real lines per z-pass block, FFT
+    // columns per y/x-pass block, threads per spread/gather block.
+    int tune_[3] = {16, 8, 128};
+    std::string autotune();
     std::string build_graph(double dt, int report);
     void free_graphs();
     std::string one_step(double dt, int report);

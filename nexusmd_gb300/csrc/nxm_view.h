@@ -73,8 +73,7 @@ struct DevView {
     void *grid_cplx;     // half complex grid: float2 / double2
     void *eterm;         // influence function on the half grid: float / double
     void *twiddle;       // float2 / double2 tables, forward sign
-    double spread_margin;  // nm an atom may drift out of its cell between rebuilds
-    int spread_cap;        // points of a cell group's shared-memory sub-grid
+    int pme_block;       // threads per block of the spread and gather (tuned at set-up)
     int4 *pme_idx;       // per slot grid base index (x, y, z)
     void *pme_frac;      // per slot fraction: float4 / double4-as-2xdouble2
     // energies, flags, report snapshot (original order, AoS [N][3])
@@ -97,7 +96,6 @@ void launch_pme(const DevView &v, const struct FftPlan &plan, int energy, cudaSt
 void launch_spread(const DevView &v, const struct FftPlan &plan, cudaStream_t st);
 void launch_fft_convolve(const DevView &v, const struct FftPlan &plan, int energy, cudaStream_t st);
 void launch_gather(const DevView &v, const struct FftPlan &plan, cudaStream_t st);
-void spread_set_smem(int points);
 void launch_integrate(const DevView &v, double dt, int report, cudaStream_t st);
 void launch_snapshot_forces(const DevView &v, cudaStream_t st);
 void launch_remap_terms(const DevView &v, cudaStream_t st);

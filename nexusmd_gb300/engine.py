@@ -41,7 +41,8 @@ class SystemDesc(C.Structure):
 
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("skin", C.c_double), ("rebuild_interval", C.c_int32),
-                ("device", C.c_int32), ("max_neighbors", C.c_int32), ("exceptions", C.c_int32)]
+                ("device", C.c_int32), ("max_neighbors", C.c_int32), ("exceptions", C.c_int32),
+                ("autotune", C.c_int32)]
 
 
 class Energies(C.Structure):
@@ -89,6 +90,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.nxm_profile_phases.argtypes = [C.c_void_p, C.c_int32, C.c_double, dp, C.c_int32]
     L.nxm_launches_per_step.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     L.nxm_rebuild_count.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
+    L.nxm_get_tuning.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
     L.nxm_n_atoms.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
     _lib = L
     return L
@@ -266,6 +268,12 @@ class Engine:
         a, b = C.c_int32(), C.c_int32()
         _check(self._L.nxm_launches_per_step(self._h, C.byref(a), C.byref(b)), "launches")
         return a.value, b.value
+
+    def tuning(self):
+        """Launch shapes in use: (FFT lines per z block, FFT columns per y/x block, spread/gather threads)."""
+        out = (C.c_int32 * 3)()
+        _check(self._L.nxm_get_tuning(self._h, out), "get_tuning")
+        return tuple(out)
 
     def rebuilds(self):
         """Neighbour-list rebuilds since the context was created."""

@@ -262,6 +262,21 @@ def test_batched_uneven_systems_match_per_system_oracle(oracle):
         eng.close()
 
 
+def test_contexts_of_different_sizes_coexist():
+    """Per-kernel launch limits are process-wide: a context created after a
+    larger one must not make the larger one's launches fail."""
+    big = sy.with_exceptions(sy.config_system(2))
+    small = sy.with_exceptions(sy.config_system(1))
+    e1 = _engine(big, precision=1, skin=0.1, rebuild_interval=10, box="explicit", exceptions=True)
+    F1 = e1.compute_forces()
+    e2 = _engine(small, precision=1, skin=0.1, rebuild_interval=10, box="explicit", exceptions=True, grid=(16, 16, 16))
+    e2.compute_forces()
+    F1b = e1.compute_forces()
+    assert np.array_equal(F1, F1b)
+    e1.close()
+    e2.close()
+
+
 def test_exceptions_bit_reproducible():
     s = sy.with_exceptions(sy.config_system(1))
     outs = []
