@@ -97,22 +97,66 @@ __global__ void k_scatter(DevView v) {
     v.new_orig[v.cell_start[key] + pos] = v.orig[s];
 }
 
-// Order inside a cell by original index, so the layout (and every sum that
-// follows it) does not depend on atomic arrival order.
-__global__ void k_cellsort(DevView v) {
+// Order inside a cell by z (the fractional box coordinate the cell binning
+// uses), ties by original index: the layout (and every sum that follows it)
+// does not depend on atomic arrival order, and each z-row of cells in a
+// staged neighbourhood is sorted by z, which lets the list build bound its
+// scan to the atom's z window.  One warp per cell: each lane ranks its
+// elements against all of the cell's (shared memory); cells of more than
+// kSortMax atoms fall back to an insertion sort by one lane.
+constexpr int kSortWarps = 4, kSortMax = 64;
+
+__global__ void __launch_bounds__(kSortWarps * 32) k_cellsort(DevView v) {
     if (!v.flags->rebuild) return;
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ double s_key[kSortWarps][kSortMax];
+    __shared__ int s_org[kSortWarps][kSortMax];
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int c = blockIdx.x * kSortWarps + warp;
     if (c >= v.total_cells) return;
-    int a = v.cell_start[c], b = v.cell_start[c + 1];
-    for (int i = a + 1; i < b; ++i) {
-        int key = v.new_orig[i];
-        int j = i - 1;
-        while (j >= a && v.new_orig[j] > key) {
-            v.new_orig[j + 1] = v.new_orig[j];
-            --j;
-        }
-        v.new_orig[j + 1] = key;
+    int a = v.cell_start[c], n = v.cell_start[c + 1] - a;
+    if (n <= 1) return;
+    auto key_of = [&](int o) {
+        int s = v.slot_of[o];
+        const SysDev &S = v.sys[v.sys_of[s]];
+        double u = (v.z[s] - S.lb[2]) * S.invL[2];
+        return u - floor(u);
+    };
+    if (n > kSortMax) {
+        if (lane == 0)
+            for (int i = a + 1; i < a + n; ++i) {
+                int o = v.new_orig[i];
+                double k = key_of(o);
+                int j = i - 1;
+                while (j >= a) {
+                    int oj = v.new_orig[j];
+                    double kj = key_of(oj);
+                    if (kj < k || (kj == k && oj < o)) break;
+                    v.new_orig[j + 1] = oj;
+                    --j;
+                }
+                v.new_orig[j + 1] = o;
+            }
+        return;
     }
+    for (int e = lane; e < n; e += 32) {
+        int o = v.new_orig[a + e];
+        s_org[warp][e] = o;
+        s_key[warp][e] = key_of(o);
+    }
+    __syncwarp();
+    int dst[2], val[2], m = 0;
+    for (int e = lane; e < n; e += 32) {
+        double k = s_key[warp][e];
+        int o = s_org[warp][e], r = 0;
+        for (int f = 0; f < n; ++f) {
+            double kf = s_key[warp][f];
+            r += kf < k || (kf == k && s_org[warp][f] < o);
+        }
+        dst[m] = r;
+        val[m] = o;
+        ++m;
+    }
+    for (int t = 0; t < m; ++t) v.new_orig[a + dst[t]] = val[t];
 }
 
 constexpr int kPermArrays = 11;
@@ -223,7 +267,7 @@ void launch_nlist_rebuild(const DevView &v, cudaStream_t st) {
     k_assign<<<blocks(v.N, 256), 256, 0, st>>>(v);
     k_scan<<<1, 1024, 0, st>>>(v.flags, v.cell_count, v.cell_start, v.total_cells);
     k_scatter<<<blocks(v.N, 256), 256, 0, st>>>(v);
-    k_cellsort<<<blocks(v.total_cells, 128), 128, 0, st>>>(v);
+    k_cellsort<<<blocks(v.total_cells, kSortWarps), kSortWarps * 32, 0, st>>>(v);
     k_permute_gather<<<blocks(v.N, 256), 256, 0, st>>>(v);
     k_permute_scatter<<<blocks(v.N, 256), 256, 0, st>>>(v);
     k_derive<<<blocks(v.N, 256), 256, 0, st>>>(v, 1);

@@ -148,8 +148,10 @@ __device__ __forceinline__ void hood_cell_bounds(const DevView &v, const SysDev 
 // radius that is not i itself and not excluded is appended to i's list as
 // its 16-bit tile index (ballot compaction: deterministic order).  An atom
 // scans only the rows of the neighbourhood its list sphere reaches, and in
-// each row only the z-cells it reaches (with a 0.01 nm margin over the cell
-// bounds), in tile order: the list is the one a scan of the whole tile gives.
+// each row (z-sorted: k_cellsort orders every cell by z) only the atoms
+// within the z extent the sphere has over that row, found by binary search
+// (0.01 nm margin), in tile order: the list is the one a scan of the whole
+// tile gives.
 __global__ void __launch_bounds__(kHoodWarps * 32) k_build(DevView v) {
     extern __shared__ __align__(16) unsigned char smem[];
     if (!v.flags->rebuild) return;
@@ -217,6 +219,27 @@ __global__ void __launch_bounds__(kHoodWarps * 32) k_build(DevView v) {
                     const int *b = s_bnd + lane * (kRowCells + 1);
                     kb = b[zlo + 2];
                     ke = b[zhi + 3];
+                    // the row is sorted by z (cells in z order, atoms in a
+                    // cell by z): narrow to the atoms with z in pz +- h
+                    const float zl = pi3[2] - h, zh = pi3[2] + h;
+                    int l = kb, r = ke;
+                    while (l < r) {
+                        int mid = (l + r) >> 1;
+                        if (s_q[mid].z < zl)
+                            l = mid + 1;
+                        else
+                            r = mid;
+                    }
+                    kb = l;
+                    r = ke;
+                    while (l < r) {
+                        int mid = (l + r) >> 1;
+                        if (s_q[mid].z <= zh)
+                            l = mid + 1;
+                        else
+                            r = mid;
+                    }
+                    ke = l;
                 }
             }
         }
