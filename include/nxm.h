@@ -96,6 +96,14 @@ typedef struct {
     int32_t autotune;         /* 1 (default): at creation, time candidate launch shapes that
                                  change no result (FFT blocking, spread/gather block size)
                                  and keep the fastest; see nxm_get_tuning */
+    int32_t report_threads;   /* Simulate only: 0 = write each report before the next step,
+                                 as the reference (Engine.cpp:162-188); N > 0 (default 4) =
+                                 copy report snapshots into pinned double buffers and write
+                                 the files on a host thread, PVF lines formatted by N threads,
+                                 while the GPU steps on.  The files are byte-identical. */
+    int32_t state_velocities; /* Simulate only: 1 = start from the state XML's <Velocities>
+                                 when it has one per atom; 0 (default) = zero velocities,
+                                 as the reference */
 } nxm_options;
 
 /* Energies of one system (kJ/mol) at the last evaluation that computed them. */
@@ -193,6 +201,22 @@ int nxm_parsed_arrays(const nxm_parsed *p, double *masses, double *positions, in
                       double *bond_params, int32_t *angle_atoms, double *angle_params,
                       int32_t *torsion_atoms, double *torsion_params, int32_t *torsion_per,
                       double *q_sig_eps, int32_t *exception_atoms, double *exception_params);
+
+/* <Velocities> of the parsed state file (OpenMM writes them beside the
+ * positions; the reference's StateXMLParser.cpp:17-37 reads positions only):
+ * *n_out = atoms with a velocity (0 when the file has none); vel ([n][3],
+ * nm/ps) may be NULL to ask for the count. */
+int nxm_parsed_velocities(const nxm_parsed *p, double *vel, int64_t *n_out);
+
+/* ---- State files (checkpoints).  OpenMM's state format: <PeriodicBoxVectors>
+ * (orthorhombic edges), <Positions> (nm) and <Velocities> (nm/ps, skipped when
+ * vel is NULL), every value with 17 significant digits, so nxm_parse_files /
+ * nxm_parsed_velocities read back the same doubles. */
+int nxm_write_state_xml(const char *path, int32_t n_atoms, const double *xyz, const double *vel,
+                        const double box[3], int64_t step, double time_ps);
+/* The current positions and velocities of one system of a context, written
+ * as above (box edges = the system's box). */
+int nxm_save_state(nxm_ctx *ctx, int32_t system, const char *path, int64_t step, double time_ps);
 
 /* ---- TaskDispatcher (TaskDispatcher.h:9-43).  "GPU" / "CUDA" select the
  * CUDA engine; any other string prints the reference's complaint and also

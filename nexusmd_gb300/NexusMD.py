@@ -27,7 +27,7 @@ from .engine import load_library
 class _Opts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("skin", C.c_double), ("rebuild_interval", C.c_int32),
                 ("device", C.c_int32), ("max_neighbors", C.c_int32), ("exceptions", C.c_int32),
-                ("autotune", C.c_int32)]
+                ("autotune", C.c_int32), ("report_threads", C.c_int32), ("state_velocities", C.c_int32)]
 
 
 def _lib():
@@ -48,6 +48,8 @@ def _lib():
         L.nxm_parsed_counts.argtypes = [vp, np.ctypeslib.ndpointer(np.int64)]
         L.nxm_parsed_nonbonded.argtypes = [vp, np.ctypeslib.ndpointer(np.float64)]
         L.nxm_parsed_arrays.argtypes = [vp] + [vp] * 12
+        L.nxm_parsed_velocities.argtypes = [vp, vp, C.POINTER(C.c_int64)]
+        L.nxm_write_state_xml.argtypes = [C.c_char_p, C.c_int32, vp, vp, vp, C.c_int64, C.c_double]
         L._nexusmd_bound = True
     return L
 
@@ -175,6 +177,11 @@ class _Parsed:
             L.nxm_parsed_arrays(h, *[a.ctypes.data if a.size else None for a in arrs])
             self.nb = np.zeros(11)
             L.nxm_parsed_nonbonded(h, self.nb)
+            nv = C.c_int64(0)
+            L.nxm_parsed_velocities(h, None, C.byref(nv))
+            self.velocities = np.zeros((nv.value, 3))
+            if nv.value:
+                L.nxm_parsed_velocities(h, self.velocities.ctypes.data, C.byref(nv))
         finally:
             L.nxm_parsed_free(h)
 
@@ -225,6 +232,25 @@ class StateXMLParser:
     def parseStateXML(filename):
         return [Coords3D(*r) for r in _Parsed(None, filename).positions]
 
+    @staticmethod
+    def parseStateVelocities(filename):
+        """The state file's <Velocities> (nm/ps), which the reference does not read;
+        empty when the file has none."""
+        return [Coords3D(*r) for r in _Parsed(None, filename).velocities]
+
+    @staticmethod
+    def writeStateXML(filename, positions, velocities=None, box=(0.0, 0.0, 0.0), step=0, time=0.0):
+        """Checkpoint in OpenMM's state format (17 significant digits: reading it back
+        gives the same doubles)."""
+        L = _lib()
+        x = np.ascontiguousarray(np.asarray([tuple(p) for p in positions], np.float64).reshape(-1, 3))
+        v = None if velocities is None else np.ascontiguousarray(
+            np.asarray([tuple(p) for p in velocities], np.float64).reshape(-1, 3))
+        b = np.ascontiguousarray(np.asarray(box, np.float64).reshape(3))
+        rc = L.nxm_write_state_xml(str(filename).encode(), len(x), x.ctypes.data,
+                                   None if v is None else v.ctypes.data, b.ctypes.data, int(step), float(time))
+        _err(L, rc, "writeStateXML")
+
 
 # ---------------------------------------------------------- dispatcher
 
@@ -266,13 +292,17 @@ class TaskDispatcher:
         self._L.nxm_dispatcher_enable_nonbonded_force(self._h)
 
     def SetOptions(self, precision="mixed", skin=0.1, rebuild_interval=10, device=0, max_neighbors=0,
-                   exceptions=False, autotune=True):
+                   exceptions=False, autotune=True, report_threads=4, state_velocities=False):
         """Engine settings the reference hard-codes (precision "mixed" or "fp64").
         exceptions=True applies the system XML's <Exceptions> (scaled 1-4 pairs,
         OpenMM semantics), which the reference parses but ignores; autotune
-        times result-neutral launch shapes at set-up and keeps the fastest."""
+        times result-neutral launch shapes at set-up and keeps the fastest;
+        report_threads > 0 writes the report files on a host thread while the
+        GPU steps on (0: before the next step, as the reference; same bytes);
+        state_velocities=True starts from the state file's <Velocities>."""
         o = _Opts(PRECISIONS[precision], float(skin), int(rebuild_interval), int(device), int(max_neighbors),
-                  1 if exceptions else 0, 1 if autotune else 0)
+                  1 if exceptions else 0, 1 if autotune else 0, int(report_threads),
+                  1 if state_velocities else 0)
         _err(self._L, self._L.nxm_dispatcher_set_options(self._h, C.byref(o)), "SetOptions")
 
     def Simulate(self, systemFilename, stateFilename, inputFilename, outputFilename, StepSize, TotalSteps,

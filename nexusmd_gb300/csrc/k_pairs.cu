@@ -53,14 +53,19 @@ __device__ __forceinline__ void i_in_group_frame(const DevView &v, const SysDev 
 }
 
 // Stage the group's neighbourhood: positions shifted into the group frame
-// (.w = scaled charge in mixed mode), LJ parameters (mixed), and for the
-// build also slots and original indices.
+// (.w = scaled charge in mixed mode), LJ parameters (pair kernel), original
+// indices (build).  Each atom's own-cell offset is shifted by its cell's
+// displacement from the group's first cell, -(ox, oy, oz) * cell edge
+// (table v.dtab; a span's cells are consecutive in z, so the code is the
+// span's first code plus the z step).  In mixed mode each lane loads four
+// atoms of its span before it stores any, so the loads of a span are in
+// flight together.
 template <bool BUILD, bool MIXED>
 __device__ int stage(const DevView &v, const SysDev &S, int sys, int c3_first, int g, float4 *s_q, float2 *s_lj,
-                     int *s_slot, int *s_orig, HoodSpan *spans, int *s_n) {
-    int n = hood_spans(v, S, c3_first, g, spans, s_n);
-    int nsp = min(s_n[1], kMaxSpans);
-    if (n > v.hood_cap || s_n[1] > kMaxSpans) {
+                     int *s_orig, HoodSpan *spans, int *s_n, int *bnd) {
+    int n = hood_setup(v, S, c3_first, g, spans, s_n, bnd);
+    int nsp = s_n[1];
+    if (n > v.hood_cap || nsp > kMaxSpans) {
         if (threadIdx.x == 0) atomicOr(&v.flags->error, ERR_NLIST_OVERFLOW);
         return -1;
     }
@@ -68,28 +73,48 @@ __device__ int stage(const DevView &v, const SysDev &S, int sys, int c3_first, i
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int sp = warp; sp < nsp; sp += nw) {
         HoodSpan h = spans[sp];
-        for (int t = lane; t < h.count; t += 32) {
-            int j = h.start + t, k = h.offset + t;
-            int cj = v.cell3[j];
-            float4 D = __ldg(dt + h.code0 + (((cj >> 20) & 1023) - h.cz0));
-            if (BUILD || MIXED) {
-                float q3[3];
-                float w = 0.f;
-                if (MIXED) {
-                    float4 p = v.pf[j];
-                    q3[0] = p.x;
-                    q3[1] = p.y;
-                    q3[2] = p.z;
-                    w = p.w;
-                } else {
-                    offset_in_cell(v, S, j, cj, q3);
+        if (MIXED) {
+            constexpr int U = 4;
+            for (int t0 = 0; t0 < h.count; t0 += 32 * U) {
+                int cj[U], oj[U];
+                float4 p[U];
+                float2 l[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    int t = t0 + lane + 32 * u;
+                    if (t < h.count) {
+                        int j = h.start + t;
+                        cj[u] = v.cell3[j];
+                        p[u] = v.pf[j];
+                        if (BUILD)
+                            oj[u] = v.orig[j];
+                        else
+                            l[u] = v.ljf[j];
+                    }
                 }
-                s_q[k] = make_float4(q3[0] - D.x, q3[1] - D.y, q3[2] - D.z, w);
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    int t = t0 + lane + 32 * u;
+                    if (t < h.count) {
+                        int k = h.offset + t;
+                        float4 D = __ldg(dt + h.code0 + (((cj[u] >> 20) & 1023) - h.cz0));
+                        s_q[k] = make_float4(p[u].x - D.x, p[u].y - D.y, p[u].z - D.z, p[u].w);
+                        if (BUILD)
+                            s_orig[k] = oj[u];
+                        else
+                            s_lj[k] = l[u];
+                    }
+                }
             }
-            if (MIXED && !BUILD) s_lj[k] = v.ljf[j];
-            if (BUILD) {
-                if (s_slot) s_slot[k] = j;
-                s_orig[k] = v.orig[j];
+        } else {
+            for (int t = lane; t < h.count; t += 32) {
+                int j = h.start + t, k = h.offset + t;
+                int cj = v.cell3[j];
+                float4 D = __ldg(dt + h.code0 + (((cj >> 20) & 1023) - h.cz0));
+                float o[3];
+                offset_in_cell(v, S, j, cj, o);
+                s_q[k] = make_float4(o[0] - D.x, o[1] - D.y, o[2] - D.z, 0.f);
+                if (BUILD) s_orig[k] = v.orig[j];
             }
         }
     }
@@ -103,46 +128,6 @@ __device__ int stage(const DevView &v, const SysDev &S, int sys, int c3_first, i
 __device__ __forceinline__ int list_pos(int p) { return (p & ~255) | ((p & 31) << 3) | ((p >> 5) & 7); }
 
 // ------------------------------------------------------------------ build
-
-constexpr int kRowCells = kMaxGroup + 4;  // cells of one neighbourhood row, at most
-
-// Tile index of the first atom of every cell of every neighbourhood row
-// (bnd[r * (kRowCells + 1) + oz + 2], oz = -2 .. g + 1) and of the row's end
-// (index g + 4): the same enumeration as hood_spans, so cell ranges of the
-// tile are contiguous index ranges.
-__device__ __forceinline__ void hood_cell_bounds(const DevView &v, const SysDev &S, int c3, int g, int *bnd) {
-    if (threadIdx.x < 32) {
-        int lane = threadIdx.x;
-        int ncz = S.nc[2], cz0 = (c3 >> 20) & 1023;
-        int rowkey = 0, tot = 0;
-        if (lane < 25) {
-            int nx = hood_wrap((c3 & 1023) + lane / 5 - 2, S.nc[0]);
-            int ny = hood_wrap(((c3 >> 10) & 1023) + lane % 5 - 2, S.nc[1]);
-            rowkey = S.cell_off + (nx * S.nc[1] + ny) * ncz;
-            for (int oz = -2; oz <= g + 1; ++oz) {
-                int cz = hood_wrap(cz0 + oz, ncz);
-                tot += v.cell_start[rowkey + cz + 1] - v.cell_start[rowkey + cz];
-            }
-        }
-        int off = tot;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            int a = __shfl_up_sync(0xffffffffu, off, o);
-            if (lane >= o) off += a;
-        }
-        off -= tot;
-        if (lane < 25) {
-            int *b = bnd + lane * (kRowCells + 1);
-            for (int oz = -2; oz <= g + 1; ++oz) {
-                int cz = hood_wrap(cz0 + oz, ncz);
-                b[oz + 2] = off;
-                off += v.cell_start[rowkey + cz + 1] - v.cell_start[rowkey + cz];
-            }
-            b[g + 4] = off;
-        }
-    }
-    __syncthreads();
-}
 
 // Each warp takes atoms of the group; every staged atom within the list
 // radius that is not i itself and not excluded is appended to i's list as
@@ -172,10 +157,9 @@ __global__ void __launch_bounds__(kHoodWarps * 32) k_build(DevView v) {
     HoodSpan *spans = reinterpret_cast<HoodSpan *>(s_bnd + 25 * (kRowCells + 1));
     int *s_n = reinterpret_cast<int *>(spans + kMaxSpans);
     int c3f = v.cell3[a0];
-    int n = v.mixed ? stage<true, true>(v, S, G.sys, c3f, G.ncell, s_q, nullptr, nullptr, s_orig, spans, s_n)
-                    : stage<true, false>(v, S, G.sys, c3f, G.ncell, s_q, nullptr, nullptr, s_orig, spans, s_n);
+    int n = v.mixed ? stage<true, true>(v, S, G.sys, c3f, G.ncell, s_q, nullptr, s_orig, spans, s_n, s_bnd)
+                    : stage<true, false>(v, S, G.sys, c3f, G.ncell, s_q, nullptr, s_orig, spans, s_n, s_bnd);
     if (n < 0) return;
-    hood_cell_bounds(v, S, c3f, G.ncell, s_bnd);
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     float rl2 = S.rlist2f * 1.0001f + 1e-6f;
     const float margin = 0.01f;
@@ -359,7 +343,7 @@ __global__ void __launch_bounds__(kHoodWarps * 32) k_pairs_mixed(DevView v) {
     HoodSpan *spans = reinterpret_cast<HoodSpan *>(s_lj + cap);
     int *s_n = reinterpret_cast<int *>(spans + kMaxSpans);
     int c3f = v.cell3[a0];
-    int n = stage<false, true>(v, S, G.sys, c3f, G.ncell, s_q, s_lj, nullptr, nullptr, spans, s_n);
+    int n = stage<false, true>(v, S, G.sys, c3f, G.ncell, s_q, s_lj, nullptr, spans, s_n, nullptr);
     if (n < 0) return;
     int nsp = s_n[1];
     int czf = (c3f >> 20) & 1023;
@@ -435,7 +419,7 @@ __global__ void __launch_bounds__(kHoodWarps * 32) k_pairs_fp64(DevView v) {
     if (!S.nb_on) return;
     HoodSpan *spans = reinterpret_cast<HoodSpan *>(smem);
     int *s_n = reinterpret_cast<int *>(spans + kMaxSpans);
-    int n = hood_spans(v, S, v.cell3[a0], G.ncell, spans, s_n);
+    int n = hood_setup(v, S, v.cell3[a0], G.ncell, spans, s_n, nullptr);
     if (n > v.hood_cap || s_n[1] > kMaxSpans) {
         if (threadIdx.x == 0) atomicOr(&v.flags->error, ERR_NLIST_OVERFLOW);
         return;
@@ -516,7 +500,7 @@ __global__ void k_collect(DevView v, int sys_sel, int *out, long long cap, unsig
     if (!S.nb_on) return;
     HoodSpan *spans = reinterpret_cast<HoodSpan *>(smem);
     int *s_n = reinterpret_cast<int *>(spans + kMaxSpans);
-    hood_spans(v, S, v.cell3[a0], G.ncell, spans, s_n);
+    hood_setup(v, S, v.cell3[a0], G.ncell, spans, s_n, nullptr);
     if (s_n[1] > kMaxSpans) return;
     int nsp = s_n[1];
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;

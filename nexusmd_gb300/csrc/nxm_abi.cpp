@@ -6,6 +6,7 @@
 
 #include "../../include/nxm.h"
 #include "nxm_engine.h"
+#include "nxm_io.h"
 
 struct nxm_ctx {
     nxm::Engine eng;
@@ -37,6 +38,8 @@ void nxm_default_options(nxm_options *opt) {
     opt->max_neighbors = 0;
     opt->exceptions = 0;
     opt->autotune = 1;
+    opt->report_threads = 4;
+    opt->state_velocities = 0;
 }
 
 static int code_for(const std::string &e) {
@@ -166,6 +169,20 @@ int nxm_get_forces(nxm_ctx *ctx, double *xyz) {
 int nxm_get_state(nxm_ctx *ctx, double *xyz, double *vel) {
     if (!ctx) return fail(NXM_ERR_INVALID, "null argument");
     NXM_CALL(ctx->eng.get_state(xyz, vel));
+}
+
+int nxm_save_state(nxm_ctx *ctx, int32_t system, const char *path, int64_t step, double time_ps) {
+    if (!ctx || !path || system < 0 || system >= ctx->eng.n_systems()) return fail(NXM_ERR_INVALID, "bad argument");
+    int n = ctx->eng.n_total();
+    std::vector<double> x(3 * (size_t)n), v(3 * (size_t)n);
+    std::string e = ctx->eng.get_state(x.data(), v.data());
+    if (!e.empty()) return fail(code_for(e), e);
+    const nxm::SysHost &h = ctx->eng.sys(system);
+    double box[3] = {h.L[0], h.L[1], h.L[2]};
+    size_t o = 3 * (size_t)h.atom_off;
+    if (!nxm::write_state_xml(path, h.natoms, x.data() + o, v.data() + o, box, (long long)step, time_ps))
+        return fail(NXM_ERR_IO, std::string("cannot write ") + path);
+    return NXM_OK;
 }
 
 int nxm_get_energies(nxm_ctx *ctx, int32_t system, nxm_energies *out) {

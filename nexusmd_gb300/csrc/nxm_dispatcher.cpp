@@ -6,7 +6,11 @@
 // Engine::RunSimulation / Engine::Report (core/baseline/src/Engine.cpp:117-188):
 // parse the inputs, box from the atom extent, velocities zero, exclusions
 // from the bonds (three bonds deep), then per step CalculateForces -> Report
-// on step 0 and every `interval`-th step -> Integrate.
+// on step 0 and every `interval`-th step -> Integrate.  With report_threads
+// > 0 the report files are written by a host thread from pinned copies of
+// the report step's snapshot while the GPU steps on (nxm_report.h); the
+// bytes are those of the synchronous loop.  state_velocities = 1 starts from
+// the state file's <Velocities> instead of zero.
 #include <cstring>
 #include <iostream>
 #include <memory>
@@ -17,6 +21,7 @@
 #include "../../include/nexusmd/TaskDispatcher.h"
 #include "nxm_engine.h"
 #include "nxm_io.h"
+#include "nxm_report.h"
 
 namespace nxm {
 extern thread_local std::string g_last_error;
@@ -94,8 +99,35 @@ public:
         auto eng = std::make_unique<nxm::Engine>();
         std::string err = eng->init({h}, opt, ps.positions.data());
         if (!err.empty()) throw std::runtime_error(err);
+        if (opt.state_velocities && ps.velocities.size() == ps.positions.size()) {
+            err = eng->set_velocities(ps.velocities.data());
+            if (!err.empty()) throw std::runtime_error(err);
+        }
 
         nxm::ReportWriter rep(inputFilename, outputFilename);
+        if (opt.report_threads > 0) {
+            // reports written by a host thread while the GPU steps on
+            nxm::AsyncReporter ar(*eng, rep, n, opt.report_threads);
+            err = ar.init();
+            if (!err.empty()) throw std::runtime_error(err);
+            for (int step = 0; step < TotalSteps; ++step) {
+                int report = (((step + 1) % interval) == 0) || step == 0;
+                err = eng->launch_step(StepSize, report);
+                if (!err.empty()) throw std::runtime_error(err);
+                if (report) {
+                    int model = (step + 1) / interval;
+                    std::cout << model << "   ";
+                    err = ar.submit(step, model);
+                    if (!err.empty()) throw std::runtime_error(err);
+                }
+                std::cout << "Simulation Step #" << step + 1 << " is completed" << std::endl;
+            }
+            err = ar.drain();
+            if (!err.empty()) throw std::runtime_error(err);
+            err = eng->sync();
+            if (!err.empty()) throw std::runtime_error(err);
+            return;
+        }
         std::vector<double> x(3 * (size_t)n), v(3 * (size_t)n), f(3 * (size_t)n);
         for (int step = 0; step < TotalSteps; ++step) {
             int report = (((step + 1) % interval) == 0) || step == 0;
@@ -211,6 +243,22 @@ int nxm_parsed_counts(const nxm_parsed *p, int64_t counts[7]) {
     counts[4] = (int64_t)p->ps.torsions.size();
     counts[5] = (int64_t)p->ps.nb.particles.size();
     counts[6] = (int64_t)p->ps.nb.exceptions.size();
+    return NXM_OK;
+}
+
+int nxm_parsed_velocities(const nxm_parsed *p, double *vel, int64_t *n_out) {
+    if (!p || !n_out) return fail(NXM_ERR_INVALID, "null argument");
+    *n_out = (int64_t)p->ps.velocities.size() / 3;
+    if (vel && !p->ps.velocities.empty())
+        std::memcpy(vel, p->ps.velocities.data(), sizeof(double) * p->ps.velocities.size());
+    return NXM_OK;
+}
+
+int nxm_write_state_xml(const char *path, int32_t n_atoms, const double *xyz, const double *vel, const double box[3],
+                        int64_t step, double time_ps) {
+    if (!path || !xyz || !box || n_atoms < 0) return fail(NXM_ERR_INVALID, "bad argument");
+    if (!nxm::write_state_xml(path, n_atoms, xyz, vel, box, (long long)step, time_ps))
+        return fail(NXM_ERR_IO, std::string("cannot write ") + path);
     return NXM_OK;
 }
 

@@ -184,6 +184,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return "no CUDA device";
     if (opt.device < 0 || opt.device >= ndev) return "bad device ordinal";
     cudaSetDevice(opt.device);
+    device_ = opt.device;
     mixed_ = opt.precision == NXM_PRECISION_MIXED ? 1 : 0;
     interval_ = opt.rebuild_interval > 0 ? opt.rebuild_interval : 1;
     int S = (int)systems.size();
@@ -932,10 +933,24 @@ std::string Engine::finish_call() {
     cudaError_t e = cudaStreamSynchronize(st_);
     if (e != cudaSuccess) return std::string("device: ") + cudaGetErrorString(e);
     for (size_t k = 0; k < energies_.size(); ++k) energies_[k] = (double)h_E_[k] * kEnergyUnscale;
-    int err = h_flags_[0];
+    return flag_error(h_flags_[0]);
+}
+
+std::string Engine::flag_error(int err) {
     if (err & ERR_NLIST_OVERFLOW) return "neighbour list capacity exceeded (raise max_neighbors)";
     if (err & ERR_NONFINITE) return "non-finite force";
     return "";
+}
+
+std::string Engine::enqueue_report(double *x, double *v, double *f, long long *E, int *flags, cudaEvent_t done) {
+    size_t b = sizeof(double) * 3 * (size_t)N_;
+    cudaMemcpyAsync(x, v_.snap_x, b, cudaMemcpyDeviceToHost, st_);
+    cudaMemcpyAsync(v, v_.snap_v, b, cudaMemcpyDeviceToHost, st_);
+    cudaMemcpyAsync(f, v_.snap_f, b, cudaMemcpyDeviceToHost, st_);
+    cudaMemcpyAsync(E, v_.E, sizeof(long long) * energies_.size(), cudaMemcpyDeviceToHost, st_);
+    cudaMemcpyAsync(flags, v_.flags, sizeof(Flags), cudaMemcpyDeviceToHost, st_);
+    cudaEventRecord(done, st_);
+    return check("report copies");
 }
 
 std::string Engine::step(int nsteps, double dt) {
@@ -1053,9 +1068,15 @@ std::string Engine::get_state(double *x, double *v) {
     return check("state");
 }
 
-void Engine::energies(int s, nxm_energies *out) const {
-    const double *e = energies_.data() + (size_t)s * E_SLOTS;
-    const SysHost &H = sysh_[s];
+void Engine::energies_from(const long long *raw, int s, nxm_energies *out) const {
+    double e[E_SLOTS];
+    for (int k = 0; k < E_SLOTS; ++k) e[k] = (double)raw[(size_t)s * E_SLOTS + k] * kEnergyUnscale;
+    decode_energies(e, sysh_[s], out);
+}
+
+void Engine::energies(int s, nxm_energies *out) const { decode_energies(energies_.data() + (size_t)s * E_SLOTS, sysh_[s], out); }
+
+void Engine::decode_energies(const double *e, const SysHost &H, nxm_energies *out) {
     std::memset(out, 0, sizeof(*out));
     out->bond = e[E_BOND];
     out->angle = e[E_ANGLE];

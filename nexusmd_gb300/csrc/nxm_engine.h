@@ -63,6 +63,21 @@ public:
         return report ? finish_call() : std::string();
     }
     std::string sync() { return finish_call(); }
+    // One step enqueued on the engine stream, not waited for; report != 0
+    // computes the step's energies and x/v/F snapshot.
+    std::string launch_step(double dt, int report) { return one_step(dt, report); }
+    // Enqueues, behind the work already on the engine stream, copies of the
+    // last report step's snapshot (x, v, F in original atom order, 3N
+    // doubles each), the raw energy accumulators (energy_words() fixed-point
+    // words) and the device flags (8 ints) into caller-owned pinned host
+    // buffers, then records `done`.  Nothing waits.
+    std::string enqueue_report(double *x, double *v, double *f, long long *E, int *flags, cudaEvent_t done);
+    int energy_words() const { return (int)energies_.size(); }
+    // Energies of system s from accumulators copied by enqueue_report.
+    void energies_from(const long long *raw, int s, nxm_energies *out) const;
+    // The error a device flags word reports ("" for none).
+    static std::string flag_error(int err);
+    int device() const { return device_; }
     std::string get_snapshot(double *x, double *v, double *f);
     std::string get_state(double *x, double *v);
     void energies(int sys, nxm_energies *out) const;
@@ -99,6 +114,7 @@ private:
     std::string one_step(double dt, int report);
     std::string check(const char *what);
     std::string finish_call();
+    static void decode_energies(const double *e, const SysHost &H, nxm_energies *out);
     void fetch_energies();
 
     DevView v_{};
@@ -109,6 +125,7 @@ private:
     cudaStream_t st_pme_ = nullptr;  // PME branch of the step graph (captured only)
     cudaEvent_t ev_fork_ = nullptr, ev_join_ = nullptr;
     int N_ = 0;
+    int device_ = 0;
     int mixed_ = 1;
     int interval_ = 1;
     bool force_rebuild_ = true;

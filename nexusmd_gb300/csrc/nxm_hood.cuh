@@ -6,12 +6,11 @@
 // atom within the list radius of any atom of the group).  In slot order the
 // cells of one (ox, oy) row are adjacent, so the neighbourhood is a few
 // contiguous slot spans per row, enumerated in a fixed order: rows
-// ox = -2..2, oy = -2..2, then z merged into spans.  Entry k of the staged
-// tile is the k-th atom of that enumeration and neighbour lists store k
-// (16 bits), so the pair kernel reads j from shared memory rather than by
-// scattered global loads.  Positions are staged already shifted into the
-// frame of the group's first cell (the cell-image displacement is applied
-// while loading), so a pair displacement is one subtraction.
+// ox = -2..2, oy = -2..2, then z.  Entry k of the staged tile is the k-th
+// atom of that enumeration and neighbour lists store k (16 bits), so the
+// pair kernel reads j from shared memory rather than by scattered global
+// loads.  Positions are staged shifted into the frame of the group's first
+// cell, so a pair displacement is one subtraction.
 #pragma once
 
 #include "nxm_view.h"
@@ -21,12 +20,13 @@ namespace nxm {
 constexpr int kHoodWarps = 16;   // warps per group block
 constexpr int kMaxSpans = 128;
 constexpr int kMaxGroup = kMaxGroupCells;
+constexpr int kRowCells = kMaxGroup + 4;  // cells of one neighbourhood row, at most
 
 struct HoodSpan {
     int start;   // first slot
     int count;   // atoms
     int offset;  // first tile index
-    int code0;   // cell-image code of the span's first cell (relative to the group's first cell)
+    int code0;   // cell-image code of the span's first cell (row * kRowCells + oz + 2)
     int cz0;     // z index of that cell
 };
 
@@ -35,59 +35,83 @@ __device__ __forceinline__ int hood_wrap(int a, int n) {
     return a < 0 ? a + n : a;
 }
 
-// Warp 0 lists the spans of the neighbourhood of the group whose first cell
-// has packed coordinates c3 and which holds g cells; every thread gets the
-// tile size after the barrier.  Cell-image codes stay in [-2, 2]^3 relative
-// to the group's first cell except along z, where they run to g + 1; the
-// displacement table is indexed by (ox+2)*25 + (oy+2)*5 + (oz+2) with oz up
-// to kMaxGroup + 1, hence its 5 x 5 x (kMaxGroup + 4) layout.
-__device__ __forceinline__ int hood_spans(const DevView &v, const SysDev &S, int c3, int g, HoodSpan *spans,
-                                          int *s_n) {
-    int ci[3] = {c3 & 1023, (c3 >> 10) & 1023, (c3 >> 20) & 1023};
+// a in (-n, 2n): one periodic shift
+__device__ __forceinline__ int wrap_once(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
+
+// Warp 0 enumerates the neighbourhood of the group whose first cell has
+// packed coordinates c3 and which holds g cells.  Lane r < 25 takes row r
+// (ox = r / 5 - 2, oy = r % 5 - 2) and reads the slot range of each of its
+// g + 4 cells at once; runs of cells adjacent in slot order become spans.
+// With bnd, it also records the tile index of the first atom of every cell
+// of every row, bnd[r * (kRowCells + 1) + oz + 2] (oz = -2 .. g + 1), and
+// of the row's end (index g + 4).  Every thread gets the tile size after
+// the barrier; s_n[1] holds the span count (above kMaxSpans: overflow).
+__device__ __forceinline__ int hood_setup(const DevView &v, const SysDev &S, int c3, int g, HoodSpan *spans,
+                                          int *s_n, int *bnd) {
     if (threadIdx.x < 32) {
+        const unsigned full = 0xffffffffu;
         int lane = threadIdx.x;
-        HoodSpan mine[4];
-        int nm = 0, tot = 0;
+        int ncz = S.nc[2], cz0 = (c3 >> 20) & 1023;
+        int rowkey = 0;
         if (lane < 25) {
-            int ox = lane / 5 - 2, oy = lane % 5 - 2;
-            int nx = hood_wrap(ci[0] + ox, S.nc[0]), ny = hood_wrap(ci[1] + oy, S.nc[1]);
-            int ncz = S.nc[2];
-            int rowkey = S.cell_off + (nx * S.nc[1] + ny) * ncz;
-            int codexy = ((ox + 2) * 5 + (oy + 2)) * (kMaxGroup + 4);
-            int ozmax = g + 1;
-            int oz = -2;
-            while (oz <= ozmax && nm < 4) {
-                int cz0 = hood_wrap(ci[2] + oz, ncz), oz0 = oz, cz = cz0;
-                while (oz < ozmax && cz + 1 < ncz && hood_wrap(ci[2] + oz + 1, ncz) == cz + 1) {
-                    ++oz;
-                    ++cz;
-                }
-                ++oz;
-                int a = v.cell_start[rowkey + cz0], b = v.cell_start[rowkey + cz + 1];
-                mine[nm].start = a;
-                mine[nm].count = b - a;
-                mine[nm].code0 = codexy + oz0 + 2;
-                mine[nm].cz0 = cz0;
-                tot += b - a;
-                ++nm;
+            int nx = hood_wrap((c3 & 1023) + lane / 5 - 2, S.nc[0]);
+            int ny = hood_wrap(((c3 >> 10) & 1023) + lane % 5 - 2, S.nc[1]);
+            rowkey = S.cell_off + (nx * S.nc[1] + ny) * ncz;
+        }
+        int a[kRowCells], b[kRowCells];
+#pragma unroll
+        for (int q = 0; q < kRowCells; ++q) {
+            a[q] = 0;
+            b[q] = 0;
+            if (lane < 25 && q < g + 4) {
+                int cz = wrap_once(cz0 + q - 2, ncz);
+                a[q] = v.cell_start[rowkey + cz];
+                b[q] = v.cell_start[rowkey + cz + 1];
             }
-            if (oz <= ozmax) tot = 1 << 24;  // more spans than the enumeration holds: reported as overflow
+        }
+        // spans: maximal runs of non-empty cells that continue one another in slot order
+        int tot = 0, nm = 0, end = -1;
+#pragma unroll
+        for (int q = 0; q < kRowCells; ++q) {
+            if (b[q] > a[q]) {
+                nm += (a[q] != end);
+                end = b[q];
+            }
+            tot += b[q] - a[q];
         }
         int nsp = nm, ntot = tot;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            int a = __shfl_up_sync(0xffffffffu, nsp, o), b = __shfl_up_sync(0xffffffffu, ntot, o);
+            int x = __shfl_up_sync(full, nsp, o), y = __shfl_up_sync(full, ntot, o);
             if (lane >= o) {
-                nsp += a;
-                ntot += b;
+                nsp += x;
+                ntot += y;
             }
         }
-        int sp0 = nsp - nm, at0 = ntot - tot;
-        for (int k = 0; k < nm; ++k) {
-            HoodSpan h = mine[k];
-            h.offset = at0;
-            at0 += h.count;
-            if (sp0 + k < kMaxSpans) spans[sp0 + k] = h;
+        int sp = nsp - nm, off = ntot - tot;
+        if (lane < 25) {
+            end = -1;
+            int cur = -1;
+            int *bd = bnd ? bnd + lane * (kRowCells + 1) : nullptr;
+#pragma unroll
+            for (int q = 0; q < kRowCells; ++q) {
+                if (q < g + 4) {
+                    if (bd) bd[q] = off;
+                    int c = b[q] - a[q];
+                    if (c > 0) {
+                        if (a[q] != end) {
+                            cur = sp++;
+                            if (cur < kMaxSpans)
+                                spans[cur] = HoodSpan{a[q], c, off, lane * kRowCells + q, wrap_once(cz0 + q - 2, ncz)};
+                        } else if (cur < kMaxSpans) {
+                            spans[cur].count += c;
+                        }
+                        end = b[q];
+                    }
+                    off += c;
+                }
+            }
+            if (bd) bd[g + 4] = off;
         }
         if (lane == 31) {
             s_n[0] = ntot;

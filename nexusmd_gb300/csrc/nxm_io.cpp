@@ -3,13 +3,16 @@
 // Reporter.cpp:26-229), producing the same values and the same file bytes.
 #include "nxm_io.h"
 
+#include <algorithm>
 #include <cctype>
 #include <cstdio>
 #include <ctime>
 #include <fstream>
+#include <functional>
 #include <iostream>
 #include <set>
 #include <sstream>
+#include <thread>
 
 #include "nxm_xml.h"
 
@@ -133,18 +136,23 @@ NbParams nonbonded_of(const XmlDoc &d) {
     return p;
 }
 
-std::vector<double> positions_of(const XmlDoc &d) {
+// <State><Positions><Position x y z/> (StateXMLParser.cpp:17-37), and the
+// same for <Velocities><Velocity/>, which OpenMM writes beside them and the
+// reference does not read.
+std::vector<double> vectors_of(const XmlDoc &d, const char *group, const char *item) {
     std::vector<double> out;
     const XmlNode *st = d.root.child("State");
-    const XmlNode *ps = st ? st->child("Positions") : nullptr;
+    const XmlNode *ps = st ? st->child(group) : nullptr;
     if (ps)
-        for (auto *q : ps->children_named("Position")) {
+        for (auto *q : ps->children_named(item)) {
             out.push_back(q->as_double("x"));
             out.push_back(q->as_double("y"));
             out.push_back(q->as_double("z"));
         }
     return out;
 }
+
+std::vector<double> positions_of(const XmlDoc &d) { return vectors_of(d, "Positions", "Position"); }
 
 }  // namespace
 
@@ -178,7 +186,10 @@ bool xml_ok(const std::string &path) { return xml_load_file(path).error.empty();
 ParsedSystem parse_all(const std::string &system_xml, const std::string &state_xml) {
     ParsedSystem ps;
     XmlDoc st;
-    if (!state_xml.empty() && load(state_xml, st)) ps.positions = positions_of(st);
+    if (!state_xml.empty() && load(state_xml, st)) {
+        ps.positions = positions_of(st);
+        ps.velocities = vectors_of(st, "Velocities", "Velocity");
+    }
     XmlDoc d;
     if (!system_xml.empty() && load(system_xml, d)) {
         ps.masses = masses_of(d);
@@ -258,13 +269,13 @@ bool ReportWriter::pdb_part1() {
     return true;
 }
 
-bool ReportWriter::pdb_part2(const double *pos, int model) {
+bool ReportWriter::pdb_part2(const double *pos, int model, bool announce) {
     std::ofstream out(out_, std::ios::out | std::ios::app);
     if (!out.is_open()) {
         std::cerr << "Unable to open the file: " << out_ << std::endl;
         return false;
     }
-    std::cout << model << "   ";
+    if (announce) std::cout << model << "   ";
     out << "MODEL        " << model << std::endl;
     for (size_t i = 0; i < tmpl_.size(); ++i) {
         PdbAtom a = tmpl_[i];
@@ -299,7 +310,7 @@ bool ReportWriter::total_energy(double ke, double pe, double te, int step) {
     return true;
 }
 
-bool ReportWriter::pvf(const double *pos, const double *vel, const double *frc, int n, int step) {
+bool ReportWriter::pvf(const double *pos, const double *vel, const double *frc, int n, int step, int threads) {
     std::string name = "PVFReport" + out_;
     std::ofstream out(name, step == 0 ? std::ios::out : (std::ios::out | std::ios::app));
     if (!out.is_open()) {
@@ -308,18 +319,66 @@ bool ReportWriter::pvf(const double *pos, const double *vel, const double *frc, 
     }
     out << "Step" << step << "\n";
     out << "ID\tPosition(nm)\t\t\tVelocity(nm / ps)\t\tForce(kJ / mol * nm)\n";
-    std::string buf;
-    buf.reserve((size_t)n * 160);
-    char line[512];
-    for (int i = 0; i < n; ++i) {
-        const double *p = pos + 3 * (size_t)i, *v = vel + 3 * (size_t)i, *f = frc + 3 * (size_t)i;
-        std::snprintf(line, sizeof line,
-                      "%d\t(%10.10f, %10.10f, %10.10f)\t(%10.10f, %10.10f, %10.10f)\t(%10.10f, %10.10f, %10.10f)\n", i + 1,
-                      p[0], p[1], p[2], v[0], v[1], v[2], f[0], f[1], f[2]);
-        buf += line;
+    auto format = [&](int i0, int i1, std::string &buf) {
+        buf.reserve((size_t)(i1 - i0) * 160);
+        char line[512];
+        for (int i = i0; i < i1; ++i) {
+            const double *p = pos + 3 * (size_t)i, *v = vel + 3 * (size_t)i, *f = frc + 3 * (size_t)i;
+            std::snprintf(line, sizeof line,
+                          "%d\t(%10.10f, %10.10f, %10.10f)\t(%10.10f, %10.10f, %10.10f)\t(%10.10f, %10.10f, %10.10f)\n",
+                          i + 1, p[0], p[1], p[2], v[0], v[1], v[2], f[0], f[1], f[2]);
+            buf += line;
+        }
+    };
+    int nt = std::max(1, std::min(threads, n / 4096 + 1));
+    std::vector<std::string> parts(nt);
+    if (nt == 1) {
+        format(0, n, parts[0]);
+    } else {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nt; ++t)
+            pool.emplace_back(format, (int)((long long)n * t / nt), (int)((long long)n * (t + 1) / nt), std::ref(parts[t]));
+        for (auto &th : pool) th.join();
     }
-    out << buf << "\n";
+    for (auto &p : parts) out << p;
+    out << "\n";
     return true;
+}
+
+bool write_state_xml(const std::string &path, int n, const double *xyz, const double *vel, const double box[3],
+                     long long step, double time_ps) {
+    std::ofstream out(path);
+    if (!out.is_open()) {
+        std::cerr << "Unable to open the file: " << path << std::endl;
+        return false;
+    }
+    std::string buf;
+    buf.reserve((size_t)n * 160 + 512);
+    char line[256];
+    std::snprintf(line, sizeof line,
+                  "<?xml version=\"1.0\" ?>\n<State stepCount=\"%lld\" time=\"%.17g\" type=\"State\" version=\"1\">\n",
+                  step, time_ps);
+    buf += line;
+    std::snprintf(line, sizeof line,
+                  "\t<PeriodicBoxVectors>\n\t\t<A x=\"%.17g\" y=\"0\" z=\"0\"/>\n\t\t<B x=\"0\" y=\"%.17g\" z=\"0\"/>\n"
+                  "\t\t<C x=\"0\" y=\"0\" z=\"%.17g\"/>\n\t</PeriodicBoxVectors>\n",
+                  box[0], box[1], box[2]);
+    buf += line;
+    const double *arr[2] = {xyz, vel};
+    const char *group[2] = {"Positions", "Velocities"}, *item[2] = {"Position", "Velocity"};
+    for (int k = 0; k < 2; ++k) {
+        if (!arr[k]) continue;
+        buf += std::string("\t<") + group[k] + ">\n";
+        for (int i = 0; i < n; ++i) {
+            const double *p = arr[k] + 3 * (size_t)i;
+            std::snprintf(line, sizeof line, "\t\t<%s x=\"%.17g\" y=\"%.17g\" z=\"%.17g\"/>\n", item[k], p[0], p[1], p[2]);
+            buf += line;
+        }
+        buf += std::string("\t</") + group[k] + ">\n";
+    }
+    buf += "</State>\n";
+    out << buf;
+    return (bool)out;
 }
 
 }  // namespace nxm

@@ -44,8 +44,15 @@ struct ParsedSystem {
     std::vector<BondP> bonds;
     std::vector<AngleP> angles;
     NbParams nb;
-    std::vector<double> positions;  // [n][3] from the state file
+    std::vector<double> positions;   // [n][3] from the state file
+    std::vector<double> velocities;  // [n][3] <Velocities> of the state file, when it has them
 };
+
+// A checkpoint in OpenMM's state format: <PeriodicBoxVectors> (orthorhombic
+// edges), <Positions> and <Velocities>, every value printed with 17
+// significant digits so that reading it back gives the same doubles.
+bool write_state_xml(const std::string &path, int n, const double *xyz, const double *vel, const double box[3],
+                     long long step, double time_ps);
 
 // Each parser mirrors one SystemXMLParser / StateXMLParser function: on a
 // file that does not parse it prints the reference's message to stderr and
@@ -80,13 +87,17 @@ public:
     // Reporter::pdbOutputGeneratorPart1: template from the input PDB, then
     // the REMARK and CRYST1 lines (file truncated).
     bool pdb_part1();
-    // Reporter::pdbOutputGeneratorPart2: one MODEL with positions x10 (nm -> A).
-    bool pdb_part2(const double *pos, int model);
+    // Reporter::pdbOutputGeneratorPart2: one MODEL with positions x10 (nm -> A);
+    // `announce` prints the model number to stdout as the reference does
+    // (a caller that reports from another thread prints it itself, in order).
+    bool pdb_part2(const double *pos, int model, bool announce = true);
     // Reporter::TotalEnergyReport: header and fixed 10-digit numbers on the
     // step-0 open only, default stream formatting afterwards.
     bool total_energy(double ke, double pe, double te, int step);
-    // Reporter::TestPVFReport.
-    bool pvf(const double *pos, const double *vel, const double *frc, int n, int step);
+    // Reporter::TestPVFReport.  The lines are formatted by `threads` threads
+    // over contiguous atom ranges and written in order: the same bytes for
+    // any thread count.
+    bool pvf(const double *pos, const double *vel, const double *frc, int n, int step, int threads = 1);
     const std::string &error() const { return err_; }
 
 private:

@@ -42,7 +42,7 @@ class SystemDesc(C.Structure):
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("skin", C.c_double), ("rebuild_interval", C.c_int32),
                 ("device", C.c_int32), ("max_neighbors", C.c_int32), ("exceptions", C.c_int32),
-                ("autotune", C.c_int32)]
+                ("autotune", C.c_int32), ("report_threads", C.c_int32), ("state_velocities", C.c_int32)]
 
 
 class Energies(C.Structure):
@@ -92,6 +92,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.nxm_rebuild_count.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
     L.nxm_get_tuning.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
     L.nxm_n_atoms.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
+    L.nxm_save_state.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_int64, C.c_double]
     _lib = L
     return L
 
@@ -280,3 +281,9 @@ class Engine:
         n = C.c_int64()
         _check(self._L.nxm_rebuild_count(self._h, C.byref(n)), "rebuild_count")
         return n.value
+
+    def save_state(self, path, system=0, step=0, time=0.0):
+        """Checkpoint of one system's current positions and velocities in OpenMM's
+        state format (17 significant digits: reading it back gives the same doubles)."""
+        _check(self._L.nxm_save_state(self._h, int(system), str(path).encode(), int(step), float(time)),
+               "save_state")

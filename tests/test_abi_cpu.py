@@ -85,3 +85,35 @@ def test_dispatcher_factory_messages(capfd):
     assert capfd.readouterr().err == ""
     NexusMD.TaskDispatcher.CreateDispatcher("CPU")
     assert "Invalid processor type" in capfd.readouterr().err
+
+
+def test_state_checkpoint_round_trip(tmp_path):
+    """nxm_write_state_xml writes OpenMM's state format with 17 significant
+    digits; the reader gives back the same doubles, positions and velocities."""
+    import NexusMD
+    rng = np.random.default_rng(5)
+    n = 257
+    x = rng.normal(0, 3.0, (n, 3)) * 10.0 ** rng.integers(-6, 3, (n, 3))
+    v = rng.normal(0, 1.0, (n, 3))
+    x[0] = [0.0, -0.0, 1e-300]
+    v[1] = [np.nextafter(1.0, 2.0), -np.pi, 6.02214076e23]
+    path = str(tmp_path / "ckpt.xml")
+    NexusMD.StateXMLParser.writeStateXML(path, [tuple(r) for r in x], [tuple(r) for r in v],
+                                         box=(3.1, 3.2, 3.3), step=1234, time=0.617)
+    px = np.array([p.data for p in NexusMD.StateXMLParser.parseStateXML(path)])
+    pv = np.array([p.data for p in NexusMD.StateXMLParser.parseStateVelocities(path)])
+    assert np.array_equal(px, x) and np.array_equal(pv, v)
+    txt = open(path).read()
+    assert '<State stepCount="1234"' in txt and '<A x="3.1000000000000001" y="0" z="0"/>' in txt
+
+
+def test_state_without_velocities(tmp_path):
+    """A state file with positions only (the reference's inputs) has no velocities."""
+    import NexusMD
+    s = sy.make_system(1, 3, 10, 2.2, seed=4)
+    sp, st, pdb = sy.write_inputs(s, str(tmp_path), "nv")
+    assert NexusMD.StateXMLParser.parseStateVelocities(st) == []
+    path = str(tmp_path / "pos_only.xml")
+    NexusMD.StateXMLParser.writeStateXML(path, [tuple(r) for r in s.pos])
+    assert "<Velocities>" not in open(path).read()
+    assert np.array_equal(np.array([p.data for p in NexusMD.StateXMLParser.parseStateXML(path)]), s.pos)

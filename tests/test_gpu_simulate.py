@@ -34,19 +34,19 @@ def _lines_match(got, ref, rtol, atol):
     return len(a) == len(b) and np.allclose(a, b, rtol=rtol, atol=atol)
 
 
-def _run(tmp_path, precision, steps, interval, idx):
+def _run(tmp_path, precision, steps, interval, idx, state=None, **opts):
     import NexusMD
     d = NexusMD.TaskDispatcher.CreateDispatcher("GPU")
     d.EnableHarmonicBondForce()
     d.EnableHarmonicAngleForce()
     d.EnablePeriodicTorsionForce()
     d.EnableNonbondedForce()
-    d.SetOptions(precision=precision, skin=0.1, rebuild_interval=10)
+    d.SetOptions(precision=precision, skin=0.1, rebuild_interval=10, **opts)
     cwd = os.getcwd()
     os.chdir(tmp_path)
     try:
         out = "out%d.pdb" % idx
-        d.Simulate(os.path.join(GOLD, "system_small.xml"), os.path.join(GOLD, "state_small.xml"),
+        d.Simulate(os.path.join(GOLD, "system_small.xml"), state or os.path.join(GOLD, "state_small.xml"),
                    os.path.join(GOLD, "small.pdb"), out, 0.0005, steps, interval)
         return {f: open(os.path.join(tmp_path, f)).read().splitlines()
                 for f in (out, "PVFReport" + out, "TotalEnergy" + out)}
@@ -115,3 +115,55 @@ def test_simulate_applies_xml_exceptions_on_request(tmp_path, oracle):
     assert E1["exception"] != 0.0
     assert abs(pe[False] - E0["reported_pe"]) <= 1e-8 * abs(E0["reported_pe"]) + 1e-6
     assert abs(pe[True] - E1["reported_pe"]) <= 1e-8 * abs(E1["reported_pe"]) + 1e-6
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_async_reporter_writes_the_synchronous_files(tmp_path, precision):
+    """report_threads > 0 (pinned double-buffered snapshot copies, files
+    written on a host thread while the GPU steps on) gives the same bytes as
+    writing each report before the next step."""
+    sync = _run(tmp_path, precision, 23, 2, 0, report_threads=0)
+    asyn = _run(tmp_path, precision, 23, 2, 1, report_threads=3)
+    for name, lines in sync.items():
+        other = asyn[name.replace("out0", "out1")]
+        assert len(other) == len(lines), name
+        for a, b in zip(lines, other):
+            if a.startswith("REMARK   Generated by"):
+                continue
+            assert a == b, (name, a, b)
+
+
+def test_simulate_starts_from_state_velocities_on_request(tmp_path):
+    """state_velocities=True takes v0 from the state file's <Velocities>: the
+    step-0 PVF velocity column is those velocities (10 decimals); without the
+    option it is zero, as the reference."""
+    import NexusMD
+    src = os.path.join(GOLD, "state_small.xml")
+    pos = NexusMD.StateXMLParser.parseStateXML(src)
+    rng = np.random.default_rng(11)
+    vel = rng.normal(0.0, 0.5, (len(pos), 3))
+    st = str(tmp_path / "state_v.xml")
+    NexusMD.StateXMLParser.writeStateXML(st, pos, [tuple(r) for r in vel])
+    for use, idx in ((True, 0), (False, 1)):
+        got = _run(tmp_path, "fp64", 1, 1, idx, state=st, state_velocities=use)
+        rows = got["PVFReportout%d.pdb" % idx][2:2 + len(pos)]
+        v = np.array([[float(x) for x in NUM.findall(r.split("\t")[2])] for r in rows])
+        assert np.allclose(v, vel if use else 0.0, rtol=0, atol=6e-11)
+
+
+def test_checkpoint_round_trip_through_engine(tmp_path):
+    """Engine.save_state writes the context's current positions and
+    velocities; reading the file back gives the same doubles."""
+    import NexusMD
+    from nexusmd_gb300 import synthetic as sy
+    from nexusmd_gb300.engine import Engine
+    s = sy.compat_system(sy.make_system(1, 4, 120, 2.9, seed=31))
+    e = Engine(s)
+    e.set_velocities(sy.maxwell_boltzmann(np.asarray(s.mass), 300.0, seed=2))
+    e.step(37, 0.0005)
+    x, v = e.state()
+    path = str(tmp_path / "ck.xml")
+    e.save_state(path, step=37, time=37 * 0.0005)
+    px = np.array([p.data for p in NexusMD.StateXMLParser.parseStateXML(path)])
+    pv = np.array([p.data for p in NexusMD.StateXMLParser.parseStateVelocities(path)])
+    assert np.array_equal(px, x) and np.array_equal(pv, v)
