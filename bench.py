@@ -315,6 +315,49 @@ def other_workload(cfg, steps, warmup, device, check=True):
     return out
 
 
+def reporting(cfg, steps, interval, device):
+    """Simulate through the dispatcher (XML inputs, the three report files):
+    wall time with each report written before the next step (report_threads
+    = 0, the reference's schedule) and with the asynchronous reporter
+    (pinned double-buffered snapshots, files written on host threads)."""
+    import shutil
+    import tempfile
+    import NexusMD
+    from nexusmd_gb300 import synthetic as sy
+    s = sy.compat_system(sy.config_system(cfg))
+    d = tempfile.mkdtemp(prefix="nxm_rep_")
+    sp, st, pdb = sy.write_inputs(s, d, "rep")
+    out = {"workload": "config%d compat inputs (%d atoms), mixed precision" % (cfg, s.n), "steps": steps,
+           "report_interval": interval, "reports": steps // interval + (interval > 1)}
+    cwd = os.getcwd()
+    saved, null = os.dup(1), os.open(os.devnull, os.O_WRONLY)
+    try:
+        os.chdir(d)
+        for th, key in ((0, "sync_s"), (4, "async_s")):
+            disp = NexusMD.TaskDispatcher.CreateDispatcher("GPU")
+            disp.EnableHarmonicBondForce()
+            disp.EnableHarmonicAngleForce()
+            disp.EnablePeriodicTorsionForce()
+            disp.EnableNonbondedForce()
+            disp.SetOptions(precision="mixed", autotune=False, report_threads=th, device=device)
+            sys.stdout.flush()
+            os.dup2(null, 1)  # Simulate prints a line per step
+            t0 = time.perf_counter()
+            try:
+                disp.Simulate(sp, st, pdb, "o%d.pdb" % th, DT_PS, steps, interval)
+            finally:
+                os.dup2(saved, 1)
+            out[key] = time.perf_counter() - t0
+            del disp
+    finally:
+        os.chdir(cwd)
+        os.close(null)
+        os.close(saved)
+        shutil.rmtree(d, ignore_errors=True)
+    out["async_speedup"] = out["sync_s"] / out["async_s"]
+    return out
+
+
 def native(args):
     import numpy as np
     from nexusmd_gb300.engine import Engine, load_library
@@ -418,6 +461,7 @@ def native(args):
             out["other_workloads"] = {
                 "c4": other_workload(4, 200, 10, local, check=not args.no_check),
                 "c5": other_workload(5, 100, 5, local, check=not args.no_check)}
+            out["simulate_reporting"] = [reporting(1, 400, 1, local), reporting(3, 100, 10, local)]
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_baseline(s, steps=args.cpu_steps)
     if rank == 0:

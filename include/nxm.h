@@ -218,6 +218,12 @@ int nxm_write_state_xml(const char *path, int32_t n_atoms, const double *xyz, co
  * as above (box edges = the system's box). */
 int nxm_save_state(nxm_ctx *ctx, int32_t system, const char *path, int64_t step, double time_ps);
 
+/* The reporters' number formatter: the text printf("%*.*f", width, prec, x)
+ * gives, written to out (cap bytes, NUL-terminated); returns its length or a
+ * negative NXM_ERR_* code.  Exact decimal rounding (half to even) in 128-bit
+ * integers for finite |x| < 2^40 and prec <= 17, snprintf otherwise. */
+int nxm_format_fixed(double x, int32_t prec, int32_t width, char *out, int32_t cap);
+
 /* ---- TaskDispatcher (TaskDispatcher.h:9-43).  "GPU" / "CUDA" select the
  * CUDA engine; any other string prints the reference's complaint and also
  * selects it (this library has no CPU engine). */

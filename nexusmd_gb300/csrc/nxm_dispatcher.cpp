@@ -262,6 +262,15 @@ int nxm_write_state_xml(const char *path, int32_t n_atoms, const double *xyz, co
     return NXM_OK;
 }
 
+int nxm_format_fixed(double x, int32_t prec, int32_t width, char *out, int32_t cap) {
+    if (!out || prec < 0 || width < 0 || width > 64) return fail(NXM_ERR_INVALID, "bad argument");
+    char buf[nxm::kFixedCharsMax];
+    int n = nxm::fixed_chars(x, prec, width, buf);
+    if (n + 1 > cap) return fail(NXM_ERR_CAPACITY, "output buffer too small");
+    std::memcpy(out, buf, (size_t)n + 1);
+    return n;
+}
+
 int nxm_parsed_nonbonded(const nxm_parsed *p, double out[11]) {
     if (!p || !out) return fail(NXM_ERR_INVALID, "null argument");
     const nxm::NbParams &n = p->ps.nb;

@@ -5,7 +5,9 @@
 
 #include <algorithm>
 #include <cctype>
+#include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <ctime>
 #include <fstream>
 #include <functional>
@@ -203,7 +205,81 @@ ParsedSystem parse_all(const std::string &system_xml, const std::string &state_x
 
 // ------------------------------------------------------------------ reports
 
+int fixed_chars(double x, int prec, int width, char *out) {
+    static const unsigned long long p10[18] = {1ULL,
+                                               10ULL,
+                                               100ULL,
+                                               1000ULL,
+                                               10000ULL,
+                                               100000ULL,
+                                               1000000ULL,
+                                               10000000ULL,
+                                               100000000ULL,
+                                               1000000000ULL,
+                                               10000000000ULL,
+                                               100000000000ULL,
+                                               1000000000000ULL,
+                                               10000000000000ULL,
+                                               100000000000000ULL,
+                                               1000000000000000ULL,
+                                               10000000000000000ULL,
+                                               100000000000000000ULL};
+    if (!(std::fabs(x) < 1099511627776.0) || prec < 0 || prec > 17 || width > 64)
+        return std::min(std::snprintf(out, kFixedCharsMax, "%*.*f", width, prec, x), kFixedCharsMax - 1);
+    unsigned long long bits;
+    std::memcpy(&bits, &x, sizeof bits);
+    const bool neg = (bits >> 63) != 0;
+    const int ex = (int)((bits >> 52) & 0x7ff);
+    unsigned long long m = bits & ((1ULL << 52) - 1);
+    int s;  // |x| = m * 2^-s, s >= 12 below 2^40
+    if (ex == 0) {
+        s = 1074;
+    } else {
+        m |= 1ULL << 52;
+        s = 1075 - ex;
+    }
+    using u128 = unsigned __int128;
+    const u128 P = (u128)m * p10[prec];  // < 2^110
+    u128 N = 0;
+    if (s < 128) {
+        N = P >> s;
+        const u128 rem = P - (N << s), half = (u128)1 << (s - 1);
+        if (rem > half || (rem == half && (N & 1))) ++N;
+    }  // else P < 2^110 < half an ulp of the last place: rounds to zero
+    unsigned long long ip = (unsigned long long)(N / p10[prec]), fp = (unsigned long long)(N % p10[prec]);
+    char tmp[64];
+    int t = 0;
+    for (int d = 0; d < prec; ++d) {
+        tmp[t++] = (char)('0' + fp % 10);
+        fp /= 10;
+    }
+    if (prec > 0) tmp[t++] = '.';
+    do {
+        tmp[t++] = (char)('0' + ip % 10);
+        ip /= 10;
+    } while (ip);
+    if (neg) tmp[t++] = '-';
+    int len = 0;
+    for (int pad = width - t; pad > 0; --pad) out[len++] = ' ';
+    while (t) out[len++] = tmp[--t];
+    out[len] = 0;
+    return len;
+}
+
 namespace {
+
+// "%d" of a non-negative int
+int uint_chars(int v, char *out) {
+    char tmp[16];
+    int t = 0;
+    do {
+        tmp[t++] = (char)('0' + v % 10);
+        v /= 10;
+    } while (v);
+    int len = 0;
+    while (t) out[len++] = tmp[--t];
+    return len;
+}
 
 const std::set<std::string> kAminoAcids = {"ALA", "ARG", "ASN", "ASP", "CYS", "GLN", "GLU", "GLY", "HIS", "ILE",
                                            "LEU", "LYS", "MET", "PHE", "PRO", "SER", "THR", "TRP", "TYR", "VAL"};
@@ -276,19 +352,50 @@ bool ReportWriter::pdb_part2(const double *pos, int model, bool announce) {
         return false;
     }
     if (announce) std::cout << model << "   ";
-    out << "MODEL        " << model << std::endl;
+    // the record's text before and after the coordinates is fixed per atom
+    if (pre_.size() != tmpl_.size()) {
+        pre_.clear();
+        post_.clear();
+        char buf[256];
+        for (const PdbAtom &a : tmpl_) {
+            std::snprintf(buf, sizeof buf, "%-6s%5d %-4s %3s %c%4d    ", a.recordType.c_str(), a.atomNum,
+                          a.atomName.c_str(), a.resName.c_str(), a.chainID, a.resSeq);
+            pre_.push_back(buf);
+            std::snprintf(buf, sizeof buf, "%6.2f%6.2f          %-2s", a.occupancy, a.tempFactor, a.element.c_str());
+            post_.push_back(buf);
+        }
+    }
+    std::string text = "MODEL        " + std::to_string(model) + "\n";
+    text.reserve(tmpl_.size() * 82 + 64);
+    std::vector<char> line(pre_.empty() ? 1 : 600 + 3 * kFixedCharsMax);
     for (size_t i = 0; i < tmpl_.size(); ++i) {
         PdbAtom a = tmpl_[i];
         for (int c = 0; c < 3; ++c) a.coords[c] = pos[3 * (size_t)(a.atomNum - 1) + c] * 10.0;
-        out << pdb_line(a) << std::endl;
+        size_t k = 0;
+        if (pre_[i].size() + post_[i].size() < 256) {
+            std::memcpy(line.data(), pre_[i].data(), pre_[i].size());
+            k = pre_[i].size();
+            for (int c = 0; c < 3; ++c) k += fixed_chars(a.coords[c], 3, 8, line.data() + k);
+            std::memcpy(line.data() + k, post_[i].data(), post_[i].size());
+            k += post_[i].size();
+        }
+        if (k > 0 && k < 256) {
+            text.append(line.data(), k);
+        } else {
+            text += pdb_line(a);  // the reference's 256-byte line buffer truncates: as it does
+        }
+        text += '\n';
         if (i == tmpl_.size() - 1) {
             char buf[128];
             std::snprintf(buf, sizeof buf, "%-6s%5d %-4s %3s %c%4d", "TER", tmpl_[i].atomNum + 1, "",
                           tmpl_[i].resName.c_str(), tmpl_[i].chainID, tmpl_[i].resSeq);
-            out << buf << std::endl;
+            text += buf;
+            text += '\n';
         }
     }
-    out << "ENDMDL" << std::endl;
+    text += "ENDMDL\n";
+    out << text;
+    out.flush();
     return true;
 }
 
@@ -319,15 +426,27 @@ bool ReportWriter::pvf(const double *pos, const double *vel, const double *frc, 
     }
     out << "Step" << step << "\n";
     out << "ID\tPosition(nm)\t\t\tVelocity(nm / ps)\t\tForce(kJ / mol * nm)\n";
+    // "%d\t(%10.10f, %10.10f, %10.10f)\t(...)\t(...)\n" per atom
     auto format = [&](int i0, int i1, std::string &buf) {
         buf.reserve((size_t)(i1 - i0) * 160);
-        char line[512];
+        char line[16 + 9 * (kFixedCharsMax + 2) + 16];
         for (int i = i0; i < i1; ++i) {
-            const double *p = pos + 3 * (size_t)i, *v = vel + 3 * (size_t)i, *f = frc + 3 * (size_t)i;
-            std::snprintf(line, sizeof line,
-                          "%d\t(%10.10f, %10.10f, %10.10f)\t(%10.10f, %10.10f, %10.10f)\t(%10.10f, %10.10f, %10.10f)\n",
-                          i + 1, p[0], p[1], p[2], v[0], v[1], v[2], f[0], f[1], f[2]);
-            buf += line;
+            const double *col[3] = {pos + 3 * (size_t)i, vel + 3 * (size_t)i, frc + 3 * (size_t)i};
+            int k = uint_chars(i + 1, line);
+            line[k++] = '\t';
+            for (int g = 0; g < 3; ++g) {
+                line[k++] = '(';
+                for (int c = 0; c < 3; ++c) {
+                    k += fixed_chars(col[g][c], 10, 10, line + k);
+                    if (c < 2) {
+                        line[k++] = ',';
+                        line[k++] = ' ';
+                    }
+                }
+                line[k++] = ')';
+                line[k++] = g < 2 ? '\t' : '\n';
+            }
+            buf.append(line, k);
         }
     };
     int nt = std::max(1, std::min(threads, n / 4096 + 1));

@@ -48,6 +48,15 @@ struct ParsedSystem {
     std::vector<double> velocities;  // [n][3] <Velocities> of the state file, when it has them
 };
 
+// printf("%*.*f", width, prec, x) without the C library's general
+// conversion: for finite |x| < 2^40 and prec <= 17 the double's exact value
+// m * 2^-s is scaled by 10^prec in 128-bit integers and rounded half to
+// even (what glibc prints under the default rounding mode), the sign of
+// negative values and of negative zero kept; anything else goes through
+// snprintf.  `out` must hold kFixedCharsMax bytes; returns the length.
+constexpr int kFixedCharsMax = 400;
+int fixed_chars(double x, int prec, int width, char *out);
+
 // A checkpoint in OpenMM's state format: <PeriodicBoxVectors> (orthorhombic
 // edges), <Positions> and <Velocities>, every value printed with 17
 // significant digits so that reading it back gives the same doubles.
@@ -103,6 +112,7 @@ public:
 private:
     std::string in_, out_, pbc_line_, err_;
     std::vector<PdbAtom> tmpl_;
+    std::vector<std::string> pre_, post_;  // each ATOM record's text around its coordinates
 };
 
 }  // namespace nxm

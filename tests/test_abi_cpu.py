@@ -117,3 +117,29 @@ def test_state_without_velocities(tmp_path):
     NexusMD.StateXMLParser.writeStateXML(path, [tuple(r) for r in s.pos])
     assert "<Velocities>" not in open(path).read()
     assert np.array_equal(np.array([p.data for p in NexusMD.StateXMLParser.parseStateXML(path)]), s.pos)
+
+
+def _fmt(L, x, prec, width):
+    buf = ctypes.create_string_buffer(512)
+    n = L.nxm_format_fixed(ctypes.c_double(x), prec, width, buf, 512)
+    assert n >= 0
+    return buf.value.decode()
+
+
+def test_report_number_formatter_matches_printf():
+    """The PVF / PDB number formatter prints what printf("%*.*f") prints:
+    random magnitudes, exact decimal ties (k / 2^11 at 10 decimals), negative
+    zero and tiny negatives, subnormals and values past the fast range."""
+    from nexusmd_gb300.engine import load_library
+    L = load_library()
+    L.nxm_format_fixed.argtypes = [ctypes.c_double, ctypes.c_int32, ctypes.c_int32, ctypes.c_char_p,
+                                   ctypes.c_int32]
+    rng = np.random.default_rng(17)
+    xs = list(rng.normal(0, 1, 4000) * 10.0 ** rng.integers(-14, 13, 4000))
+    xs += [k / 2048.0 for k in range(-3000, 3000, 7)]            # ties at 10 decimals
+    xs += [(2 * k + 1) / 2000.0 for k in range(-500, 500)]        # ties at 3 decimals, as doubles
+    xs += [0.0, -0.0, -1e-12, 1e-12, 5e-324, -5e-324, 2.0 ** 40 - 1, 2.0 ** 40, -2.0 ** 41 + 0.5,
+           1e300, -1e300, 0.5, 1.5, 2.5, -2.5, 123456.789012345678, float("inf"), float("-inf"), float("nan")]
+    for prec, width in ((10, 10), (3, 8), (2, 6), (0, 5), (17, 0)):
+        for x in xs:
+            assert _fmt(L, x, prec, width) == "%*.*f" % (width, prec, x), (x, prec, width)
