@@ -15,6 +15,7 @@
 // a safety margin); in mixed mode the FP32 r^2 settles every pair except
 // those within 1e-5 relative of the cutoff, which are re-tested in FP64.
 #include <mutex>
+#include <type_traits>
 
 #include "nxm_hood.cuh"
 #include "nxm_view.h"
@@ -40,7 +41,7 @@ __device__ __forceinline__ void offset_in_cell(const DevView &v, const SysDev &S
 // Atom i's position in the frame of the group's first cell.
 __device__ __forceinline__ void i_in_group_frame(const DevView &v, const SysDev &S, int i, int cz_first, float p[3]) {
     int c3 = v.cell3[i];
-    float gz = (float)(hood_wrap(((c3 >> 20) & 1023) - cz_first, S.nc[2])) * (float)S.cs[2];
+    float gz = (float)wrap_once(((c3 >> 20) & 1023) - cz_first, S.nc[2]) * S.csf[2];
     if (v.mixed) {
         float4 q = v.pf[i];
         p[0] = q.x;
@@ -282,9 +283,15 @@ __global__ void __launch_bounds__(kHoodWarps * 32) k_build(DevView v) {
 // ------------------------------------------------------------------ pairs
 
 struct PairPrm {
-    float alpha, sw, cut;
+    float ex2c, a04, k2a, sw, cut;  // SysDev::ex2c, a04, k2a
     int use_sw;
 };
+
+__device__ __forceinline__ float fast_ex2(float x) {
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 
 // FP32 force (and energy) of one list entry, accumulated into the lane's
 // partial sums when `in` (inside the cutoff), NonbondedForce.cpp:559-581 in
@@ -298,10 +305,12 @@ __device__ __forceinline__ void pair_mixed(bool in, float dx, float dy, float dz
     float rinv = fast_rsqrt(r2);
     float rinv2 = rinv * rinv;
     float r = r2 * rinv;
-    float xa = P.alpha * r;
-    float ex = __expf(-xa * xa);
-    float erfcv = ex * erfcx_fit(fast_rcp(fmaf(0.4f, xa, 1.0f)));
-    float dEdR = qq * rinv * rinv2 * fmaf((float)kTwoOverSqrtPi * xa, ex, erfcv);
+    // exp(-(alpha r)^2) straight from r^2; erfc(alpha r) = exp(-(alpha r)^2) g(t),
+    // t = 1 / (1 + 0.4 alpha r); 2 alpha r / sqrt(pi) as k2a * r
+    float ex = fast_ex2(r2 * P.ex2c);
+    float erfcv = ex * erfcx_fit(fast_rcp(fmaf(P.a04, r, 1.0f)));
+    float qr = qq * rinv;
+    float dEdR = qr * rinv2 * fmaf(P.k2a * r, ex, erfcv);
     float s2 = sg * sg * rinv2;
     float s6 = s2 * s2 * s2;
     float evdw = eps * (s6 - 1.0f) * s6;
@@ -321,7 +330,7 @@ __device__ __forceinline__ void pair_mixed(bool in, float dx, float dy, float dz
     fy = fmaf(dy, dEdR, fy);
     fz = fmaf(dz, dEdR, fz);
     if (ENERGY) {
-        ec += in ? qq * rinv * erfcv : 0.0f;
+        ec += in ? qr * erfcv : 0.0f;
         ev += in ? (SW ? sw * evdw : evdw) : 0.0f;
     }
 }
@@ -348,7 +357,7 @@ __global__ void __launch_bounds__(kHoodWarps * 32) k_pairs_mixed(DevView v) {
     int nsp = s_n[1];
     int czf = (c3f >> 20) & 1023;
     const float lo = S.cut2f_lo, hi = S.cut2f_hi;
-    const PairPrm P{S.alphaf, S.sw_distf, S.cutofff, S.use_switch};
+    const PairPrm P{S.ex2c, S.a04, S.k2a, S.sw_distf, S.cutofff, S.use_switch};
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     float ec = 0.f, ev = 0.f;
     for (int i = a0 + warp; i < a1; i += nw) {
@@ -364,31 +373,40 @@ __global__ void __launch_bounds__(kHoodWarps * 32) k_pairs_mixed(DevView v) {
             // this lane's entries c0 + lane + 32u, u = 0..7, and the next chunk in flight
             uint4 nxt = c0 + 256 < cnt ? __ldg(lst4 + (c0 + 256) / 8) : make_uint4(0, 0, 0, 0);
             uint32_t wds[4] = {cur.x, cur.y, cur.z, cur.w};
+            // FULL: all 256 entries of the chunk are valid (every chunk but
+            // the last), so the per-entry range checks compile away
+            auto walk = [&](auto full_chunk) {
+                constexpr bool FULL = decltype(full_chunk)::value;
 #pragma unroll
-            for (int u = 0; u < 8; u += 2) {
-            if (c0 + 32 * u >= cnt) break;  // rest of the last chunk is empty (warp-uniform)
-            int k0 = c0 + lane + 32 * u, k1 = k0 + 32;
-            bool v0 = k0 < cnt, v1 = k1 < cnt;
-            int t0 = v0 ? (int)(wds[u >> 1] & 0xffffu) : 0;
-            int t1 = v1 ? (int)(wds[u >> 1] >> 16) : 0;
-            float4 p0 = s_q[t0], p1 = s_q[t1];
-            float2 l0 = s_lj[t0], l1 = s_lj[t1];
-            float dx0 = pi3[0] - p0.x, dy0 = pi3[1] - p0.y, dz0 = pi3[2] - p0.z;
-            float dx1 = pi3[0] - p1.x, dy1 = pi3[1] - p1.y, dz1 = pi3[2] - p1.z;
-            float r20 = v0 ? dx0 * dx0 + dy0 * dy0 + dz0 * dz0 : 1e30f;
-            float r21 = v1 ? dx1 * dx1 + dy1 * dy1 + dz1 * dz1 : 1e30f;
-            bool in0 = r20 < lo, in1 = r21 < lo;
-            bool b0 = !in0 && r20 < hi, b1 = !in1 && r21 < hi;
-            if (__any_sync(full, b0 || b1)) {
-                // within 1e-5 of the cutoff: decide in FP64 exactly as the reference
-                if (b0) in0 = exact_r2(v, S, i, hood_slot(spans, nsp, t0)) < S.cut2;
-                if (b1) in1 = exact_r2(v, S, i, hood_slot(spans, nsp, t1)) < S.cut2;
-            }
-            pair_mixed<ENERGY, SW>(in0, dx0, dy0, dz0, r20, qi * p0.w, li.x + l0.x, li.y * l0.y, P, fx, fy, fz, ec,
-                                   ev);
-            pair_mixed<ENERGY, SW>(in1, dx1, dy1, dz1, r21, qi * p1.w, li.x + l1.x, li.y * l1.y, P, fx, fy, fz, ec,
-                                   ev);
-            }
+                for (int u = 0; u < 8; u += 2) {
+                    if (!FULL && c0 + 32 * u >= cnt) break;  // rest of the last chunk is empty (warp-uniform)
+                    int k0 = c0 + lane + 32 * u;
+                    bool v0 = FULL || k0 < cnt, v1 = FULL || k0 + 32 < cnt;
+                    int t0 = v0 ? (int)(wds[u >> 1] & 0xffffu) : 0;
+                    int t1 = v1 ? (int)(wds[u >> 1] >> 16) : 0;
+                    float4 p0 = s_q[t0], p1 = s_q[t1];
+                    float2 l0 = s_lj[t0], l1 = s_lj[t1];
+                    float dx0 = pi3[0] - p0.x, dy0 = pi3[1] - p0.y, dz0 = pi3[2] - p0.z;
+                    float dx1 = pi3[0] - p1.x, dy1 = pi3[1] - p1.y, dz1 = pi3[2] - p1.z;
+                    float r20 = v0 ? dx0 * dx0 + dy0 * dy0 + dz0 * dz0 : 1e30f;
+                    float r21 = v1 ? dx1 * dx1 + dy1 * dy1 + dz1 * dz1 : 1e30f;
+                    bool in0 = r20 < lo, in1 = r21 < lo;
+                    bool b0 = !in0 && r20 < hi, b1 = !in1 && r21 < hi;
+                    if (__any_sync(full, b0 || b1)) {
+                        // within 1e-5 of the cutoff: decide in FP64 exactly as the reference
+                        if (b0) in0 = exact_r2(v, S, i, hood_slot(spans, nsp, t0)) < S.cut2;
+                        if (b1) in1 = exact_r2(v, S, i, hood_slot(spans, nsp, t1)) < S.cut2;
+                    }
+                    pair_mixed<ENERGY, SW>(in0, dx0, dy0, dz0, r20, qi * p0.w, li.x + l0.x, li.y * l0.y, P, fx, fy,
+                                           fz, ec, ev);
+                    pair_mixed<ENERGY, SW>(in1, dx1, dy1, dz1, r21, qi * p1.w, li.x + l1.x, li.y * l1.y, P, fx, fy,
+                                           fz, ec, ev);
+                }
+            };
+            if (c0 + 256 <= cnt)
+                walk(std::true_type{});
+            else
+                walk(std::false_type{});
             cur = nxt;
         }
         fx = warp_sum(fx);

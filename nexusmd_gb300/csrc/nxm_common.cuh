@@ -76,7 +76,9 @@ struct SysDev {
     int nc[3], cell_off;      // neighbour cells
     double cs[3];             // cell edge
     int tw_off[3];            // twiddle-table offsets for the three FFT lengths
-    float pad_;
+    // FP32 pair-kernel constants: exp(-(alpha r)^2) = 2^(r^2 ex2c),
+    // 0.4 alpha (erfc fit argument), 2 alpha / sqrt(pi); cell edges
+    float ex2c, a04, k2a, csf[3];
 };
 
 // Flags word layout in device memory.

@@ -270,6 +270,10 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         D.cut2f_lo = (float)(D.cut2 * (1.0 - 1e-5));
         D.cut2f_hi = (float)(D.cut2 * (1.0 + 1e-5));
         D.alphaf = (float)H.alpha;
+        D.ex2c = (float)(-H.alpha * H.alpha * 1.4426950408889634);  // log2(e)
+        D.a04 = (float)(0.4 * H.alpha);
+        D.k2a = (float)(2.0 * H.alpha / kSqrtPi);
+        for (int d = 0; d < 3; ++d) D.csf[d] = (float)D.cs[d];
         D.rlist2f = (float)D.rlist2;
         D.sw_distf = (float)h.sw_dist;
         D.cutofff = (float)h.cutoff;

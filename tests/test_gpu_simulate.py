@@ -121,7 +121,11 @@ def test_simulate_applies_xml_exceptions_on_request(tmp_path, oracle):
 def test_async_reporter_writes_the_synchronous_files(tmp_path, precision):
     """report_threads > 0 (pinned double-buffered snapshot copies, files
     written on a host thread while the GPU steps on) gives the same bytes as
-    writing each report before the next step."""
+    writing each report before the next step.  The mixed engine is
+    bit-reproducible (fixed-point force sums), so its files must be equal
+    byte for byte; the FP64 engine sums forces with floating-point atomics,
+    whose order varies between runs, so there the numbers may differ in the
+    last bits."""
     sync = _run(tmp_path, precision, 23, 2, 0, report_threads=0)
     asyn = _run(tmp_path, precision, 23, 2, 1, report_threads=3)
     for name, lines in sync.items():
@@ -130,7 +134,10 @@ def test_async_reporter_writes_the_synchronous_files(tmp_path, precision):
         for a, b in zip(lines, other):
             if a.startswith("REMARK   Generated by"):
                 continue
-            assert a == b, (name, a, b)
+            if precision == "mixed":
+                assert a == b, (name, a, b)
+            else:
+                assert _lines_match(a, b, rtol=1e-11, atol=2e-10), (name, a, b)
 
 
 def test_simulate_starts_from_state_velocities_on_request(tmp_path):
