@@ -153,8 +153,8 @@ __global__ void __launch_bounds__(kHoodWarps * 32) k_build(DevView v) {
     int cap = v.hood_cap;
     float4 *s_q = reinterpret_cast<float4 *>(smem);
     int *s_orig = reinterpret_cast<int *>(s_q + cap);
-    uint16_t *s_buf = reinterpret_cast<uint16_t *>(s_orig + cap);  // [kHoodWarps][256], 16-byte aligned
-    int *s_bnd = reinterpret_cast<int *>(s_buf + kHoodWarps * 256);
+    uint16_t *s_buf = reinterpret_cast<uint16_t *>(s_orig + cap);  // [kHoodWarps][2][256], 16-byte aligned
+    int *s_bnd = reinterpret_cast<int *>(s_buf + kHoodWarps * 512);
     HoodSpan *spans = reinterpret_cast<HoodSpan *>(s_bnd + 25 * (kRowCells + 1));
     int *s_n = reinterpret_cast<int *>(spans + kMaxSpans);
     int c3f = v.cell3[a0];
@@ -183,9 +183,10 @@ __global__ void __launch_bounds__(kHoodWarps * 32) k_build(DevView v) {
         int ne = v.excl_off[oi + 1] - e0;
         int my_ex = lane < ne ? v.excl_lst[e0 + lane] : -1;
         int nfast = ne < 32 ? ne : 32;
-        // index window of the exclusion partners: candidates outside it need
-        // no membership test
-        int ex_lo = ne ? v.excl_lst[e0] : 1, ex_hi = ne ? v.excl_lst[e0 + ne - 1] : 0;
+        // index window of the exclusion partners [ex_lo, ex_lo + ex_win]:
+        // candidates outside it need no membership test (none without exclusions)
+        const int ex_lo = ne ? v.excl_lst[e0] : -1;
+        const unsigned ex_win = ne ? (unsigned)(v.excl_lst[e0 + ne - 1] - ex_lo) : 0u;
         int count = 0;
         uint16_t *out = v.nl16 + (size_t)i * v.stride;
         // lane r < 25: the tile range [kb, ke) of row r that i's sphere reaches
@@ -228,50 +229,52 @@ __global__ void __launch_bounds__(kHoodWarps * 32) k_build(DevView v) {
                 }
             }
         }
-        // the current 256-entry chunk of i's list, transposed as in memory
-        uint16_t *buf = s_buf + warp * 256;
+        // i's list is assembled per 256-entry chunk, transposed as in memory,
+        // in two halves per warp: entry p goes to half (p >> 8) & 1, so an
+        // iteration that completes a chunk writes on into the other half
+        uint16_t *buf = s_buf + warp * 512;
+        const unsigned lt = (1u << lane) - 1u;
         unsigned rows = __ballot_sync(full, ke > kb);
         while (rows) {
             int r = __ffs(rows) - 1;
             rows &= rows - 1;
-            int rb = __shfl_sync(full, kb, r), re = __shfl_sync(full, ke, r);
+            const int rb = __shfl_sync(full, kb, r), re = __shfl_sync(full, ke, r);
             for (int k0 = rb; k0 < re; k0 += 32) {
-                int k = k0 + lane;
-                bool cand = false;
-                if (k < re) {
-                    float4 q = s_q[k];
-                    float dx = pi3[0] - q.x, dy = pi3[1] - q.y, dz = pi3[2] - q.z;
-                    cand = dx * dx + dy * dy + dz * dz < rl2 && k != ki;
-                }
-                if (!__any_sync(full, cand)) continue;
-                int oj = cand ? s_orig[k] : -2;
-                bool ex = false;
-                if (__any_sync(full, cand && oj >= ex_lo && oj <= ex_hi)) {
+                const int k = k0 + lane, kk = min(k, re - 1);
+                const float4 q = s_q[kk];
+                const float dx = pi3[0] - q.x, dy = pi3[1] - q.y, dz = pi3[2] - q.z;
+                const bool cand = (k < re) & (dx * dx + dy * dy + dz * dz < rl2) & (k != ki);
+                unsigned m = __ballot_sync(full, cand);
+                if (!m) continue;
+                const int oj = s_orig[kk];
+                if (__any_sync(full, cand && (unsigned)(oj - ex_lo) <= ex_win)) {
+                    bool ex = false;
                     for (int e = 0; e < nfast; ++e) ex |= (__shfl_sync(full, my_ex, e) == oj);
                     if (ne > 32 && cand)
                         for (int e = 32; e < ne; ++e) ex |= (v.excl_lst[e0 + e] == oj);
+                    m = __ballot_sync(full, cand && !ex);
                 }
-                bool ok = cand && !ex;
-                unsigned m = __ballot_sync(full, ok);
-                int pos = count + __popc(m & ((1u << lane) - 1u));
-                int newc = count + __popc(m);
-                int cend = (count & ~255) + 256;
-                if (ok && pos < cend) buf[list_pos(pos) & 255] = (uint16_t)k;
-                if (newc >= cend) {
-                    // chunk complete: one 16-byte store per lane
+                const int pos = count + __popc(m & lt);
+                if ((m >> lane) & 1u) buf[((pos >> 8) & 1) * 256 + ((pos & 31) << 3) + ((pos >> 5) & 7)] = (uint16_t)k;
+                const int newc = count + __popc(m);
+                if ((newc ^ count) >> 8) {
+                    // chunk count >> 8 complete: one 16-byte store per lane
                     __syncwarp();
-                    if (cend <= v.stride)
-                        reinterpret_cast<uint4 *>(out + cend - 256)[lane] = reinterpret_cast<const uint4 *>(buf)[lane];
+                    const int c = count >> 8;
+                    if ((c + 1) * 256 <= v.stride)
+                        reinterpret_cast<uint4 *>(out + c * 256)[lane] =
+                            reinterpret_cast<const uint4 *>(buf + (c & 1) * 256)[lane];
                     __syncwarp();
-                    if (ok && pos >= cend) buf[list_pos(pos) & 255] = (uint16_t)k;
                 }
                 count = newc;
             }
         }
         __syncwarp();
-        int cstart = count & ~255;
-        if ((count & 255) && cstart < v.stride)
-            reinterpret_cast<uint4 *>(out + cstart)[lane] = reinterpret_cast<const uint4 *>(buf)[lane];
+        {
+            const int c = count >> 8;
+            if ((count & 255) && c * 256 < v.stride)
+                reinterpret_cast<uint4 *>(out + c * 256)[lane] = reinterpret_cast<const uint4 *>(buf + (c & 1) * 256)[lane];
+        }
         __syncwarp();
         if (lane == 0) {
             v.ncount[i] = count < v.stride ? count : v.stride;
@@ -543,7 +546,7 @@ __global__ void k_collect(DevView v, int sys_sel, int *out, long long cap, unsig
 
 static size_t tail_bytes() { return kMaxSpans * sizeof(HoodSpan) + 4 * sizeof(int); }
 static size_t smem_build(int cap) {
-    return (size_t)cap * (sizeof(float4) + sizeof(int)) + kHoodWarps * 256 * sizeof(uint16_t) +
+    return (size_t)cap * (sizeof(float4) + sizeof(int)) + kHoodWarps * 512 * sizeof(uint16_t) +
            25 * (kRowCells + 1) * sizeof(int) + tail_bytes();
 }
 static size_t smem_pairs(int cap, int mixed) {
