@@ -53,24 +53,27 @@ __device__ __forceinline__ void i_in_group_frame(const DevView &v, const SysDev 
     }
 }
 
-// Stage the group's neighbourhood: positions shifted into the group frame
-// (.w = scaled charge in mixed mode), LJ parameters (pair kernel), original
-// indices (build).  Each atom's own-cell offset is shifted by its cell's
-// displacement from the group's first cell, -(ox, oy, oz) * cell edge
-// (table v.dtab; a span's cells are consecutive in z, so the code is the
+// This system's cell-image displacements (v.dtab: code r * kRowCells +
+// oz + 2 -> -(ox, oy, oz) * cell edge) copied into shared memory by the
+// threads outside warp 0 while warp 0 enumerates the neighbourhood; read
+// after the barrier that follows.
+__device__ __forceinline__ void load_dtab(const DevView &v, int sys, float4 *s_dt) {
+    const float4 *dt = v.dtab + sys * kDtabStride;
+    for (int e = (int)threadIdx.x - 32; e < 25 * kRowCells; e += blockDim.x - 32)
+        if (e >= 0) s_dt[e] = __ldg(dt + e);
+}
+
+// Stage the group's neighbourhood (spans already in shared memory):
+// positions shifted into the group frame (.w = scaled charge in mixed mode),
+// LJ parameters (pair kernel), original indices (build).  Each atom's
+// own-cell offset is shifted by its cell's displacement from the group's
+// first cell (a span's cells are consecutive in z, so the code is the
 // span's first code plus the z step).  In mixed mode each lane loads four
 // atoms of its span before it stores any, so the loads of a span are in
 // flight together.
 template <bool BUILD, bool MIXED>
-__device__ int stage(const DevView &v, const SysDev &S, int sys, int c3_first, int g, float4 *s_q, float2 *s_lj,
-                     int *s_orig, HoodSpan *spans, int *s_n, int *bnd) {
-    int n = hood_setup(v, S, c3_first, g, spans, s_n, bnd);
-    int nsp = s_n[1];
-    if (n > v.hood_cap || nsp > kMaxSpans) {
-        if (threadIdx.x == 0) atomicOr(&v.flags->error, ERR_NLIST_OVERFLOW);
-        return -1;
-    }
-    const float4 *dt = v.dtab + sys * kDtabStride;
+__device__ void stage(const DevView &v, const SysDev &S, float4 *s_q, float2 *s_lj, int *s_orig,
+                      const HoodSpan *spans, int nsp, const float4 *s_dt) {
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int sp = warp; sp < nsp; sp += nw) {
         HoodSpan h = spans[sp];
@@ -98,7 +101,7 @@ __device__ int stage(const DevView &v, const SysDev &S, int sys, int c3_first, i
                     int t = t0 + lane + 32 * u;
                     if (t < h.count) {
                         int k = h.offset + t;
-                        float4 D = __ldg(dt + h.code0 + (((cj[u] >> 20) & 1023) - h.cz0));
+                        float4 D = s_dt[h.code0 + (((cj[u] >> 20) & 1023) - h.cz0)];
                         s_q[k] = make_float4(p[u].x - D.x, p[u].y - D.y, p[u].z - D.z, p[u].w);
                         if (BUILD)
                             s_orig[k] = oj[u];
@@ -111,7 +114,7 @@ __device__ int stage(const DevView &v, const SysDev &S, int sys, int c3_first, i
             for (int t = lane; t < h.count; t += 32) {
                 int j = h.start + t, k = h.offset + t;
                 int cj = v.cell3[j];
-                float4 D = __ldg(dt + h.code0 + (((cj >> 20) & 1023) - h.cz0));
+                float4 D = s_dt[h.code0 + (((cj >> 20) & 1023) - h.cz0)];
                 float o[3];
                 offset_in_cell(v, S, j, cj, o);
                 s_q[k] = make_float4(o[0] - D.x, o[1] - D.y, o[2] - D.z, 0.f);
@@ -120,7 +123,6 @@ __device__ int stage(const DevView &v, const SysDev &S, int sys, int c3_first, i
         }
     }
     __syncthreads();
-    return n;
 }
 
 // List layout: each 256-entry chunk of an atom's list is stored transposed,
@@ -138,7 +140,7 @@ __device__ __forceinline__ int list_pos(int p) { return (p & ~255) | ((p & 31) <
 // within the z extent the sphere has over that row, found by binary search
 // (0.01 nm margin), in tile order: the list is the one a scan of the whole
 // tile gives.
-__global__ void __launch_bounds__(kHoodWarps * 32) k_build(DevView v) {
+__global__ void __launch_bounds__(kHoodWarps * 32, 2) k_build(DevView v) {
     extern __shared__ __align__(16) unsigned char smem[];
     if (!v.flags->rebuild) return;
     const unsigned full = 0xffffffffu;
@@ -157,10 +159,26 @@ __global__ void __launch_bounds__(kHoodWarps * 32) k_build(DevView v) {
     int *s_bnd = reinterpret_cast<int *>(s_buf + kHoodWarps * 512);
     HoodSpan *spans = reinterpret_cast<HoodSpan *>(s_bnd + 25 * (kRowCells + 1));
     int *s_n = reinterpret_cast<int *>(spans + kMaxSpans);
+    __shared__ float4 s_dt[25 * kRowCells];
     int c3f = v.cell3[a0];
-    int n = v.mixed ? stage<true, true>(v, S, G.sys, c3f, G.ncell, s_q, nullptr, s_orig, spans, s_n, s_bnd)
-                    : stage<true, false>(v, S, G.sys, c3f, G.ncell, s_q, nullptr, s_orig, spans, s_n, s_bnd);
-    if (n < 0) return;
+    load_dtab(v, G.sys, s_dt);
+    int n = hood_setup(v, S, c3f, G.ncell, spans, s_n, s_bnd);
+    int nsp = s_n[1];
+    // the spans, for the pair kernel's steps until the next rebuild
+    {
+        const int *src = reinterpret_cast<const int *>(spans);
+        int *dst = v.gspan + (size_t)blockIdx.x * kGroupSpanWords;
+        for (int e = threadIdx.x; e < min(nsp, kMaxSpans) * kSpanWords; e += blockDim.x) dst[e] = src[e];
+        if (threadIdx.x == 0) v.gspan_n[blockIdx.x] = make_int2(n, nsp);
+    }
+    if (n > v.hood_cap || nsp > kMaxSpans) {
+        if (threadIdx.x == 0) atomicOr(&v.flags->error, ERR_NLIST_OVERFLOW);
+        return;
+    }
+    if (v.mixed)
+        stage<true, true>(v, S, s_q, nullptr, s_orig, spans, nsp, s_dt);
+    else
+        stage<true, false>(v, S, s_q, nullptr, s_orig, spans, nsp, s_dt);
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     float rl2 = S.rlist2f * 1.0001f + 1e-6f;
     const float margin = 0.01f;
@@ -341,7 +359,7 @@ __device__ __forceinline__ void pair_mixed(bool in, float dx, float dy, float dz
 // Mixed precision: each lane keeps two list entries in flight; j comes from
 // the staged tile.  SW: some system of the batch uses the switching function.
 template <bool ENERGY, bool SW>
-__global__ void __launch_bounds__(kHoodWarps * 32) k_pairs_mixed(DevView v) {
+__global__ void __launch_bounds__(kHoodWarps * 32, 2) k_pairs_mixed(DevView v) {
     extern __shared__ __align__(16) unsigned char smem[];
     const unsigned full = 0xffffffffu;
     CellGroup G = v.groups[blockIdx.x];
@@ -353,11 +371,26 @@ __global__ void __launch_bounds__(kHoodWarps * 32) k_pairs_mixed(DevView v) {
     float4 *s_q = reinterpret_cast<float4 *>(smem);
     float2 *s_lj = reinterpret_cast<float2 *>(s_q + cap);
     HoodSpan *spans = reinterpret_cast<HoodSpan *>(s_lj + cap);
-    int *s_n = reinterpret_cast<int *>(spans + kMaxSpans);
+    __shared__ float4 s_dt[25 * kRowCells];
+    __shared__ int2 s_nn;
     int c3f = v.cell3[a0];
-    int n = stage<false, true>(v, S, G.sys, c3f, G.ncell, s_q, s_lj, nullptr, spans, s_n, nullptr);
-    if (n < 0) return;
-    int nsp = s_n[1];
+    // the neighbourhood's spans as the list build enumerated them (the
+    // cells have not changed since), and the displacement table
+    {
+        const int *src = v.gspan + (size_t)blockIdx.x * kGroupSpanWords;
+        int *dst = reinterpret_cast<int *>(spans);
+        for (int e = threadIdx.x; e < kGroupSpanWords; e += blockDim.x) dst[e] = src[e];
+        if (threadIdx.x == 0) s_nn = v.gspan_n[blockIdx.x];
+        const float4 *dt = v.dtab + G.sys * kDtabStride;
+        for (int e = threadIdx.x; e < 25 * kRowCells; e += blockDim.x) s_dt[e] = __ldg(dt + e);
+    }
+    __syncthreads();
+    const int n = s_nn.x, nsp = s_nn.y;
+    if (n > v.hood_cap || nsp > kMaxSpans) {
+        if (threadIdx.x == 0) atomicOr(&v.flags->error, ERR_NLIST_OVERFLOW);
+        return;
+    }
+    stage<false, true>(v, S, s_q, s_lj, nullptr, spans, nsp, s_dt);
     int czf = (c3f >> 20) & 1023;
     const float lo = S.cut2f_lo, hi = S.cut2f_hi;
     const PairPrm P{S.ex2c, S.a04, S.k2a, S.sw_distf, S.cutofff, S.use_switch};

@@ -412,6 +412,8 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         }
         v_.ngroups = (int)gr.size();
         v_.groups = dalloc<CellGroup>(gr.size());
+        v_.gspan = dalloc<int>(gr.size() * (size_t)kGroupSpanWords);
+        v_.gspan_n = dalloc<int2>(gr.size());
         cudaMemcpy(v_.groups, gr.data(), sizeof(CellGroup) * gr.size(), cudaMemcpyHostToDevice);
     }
     tiles_set_smem(hood_cap);

@@ -29,6 +29,8 @@ struct HoodSpan {
     int code0;   // cell-image code of the span's first cell (row * kRowCells + oz + 2)
     int cz0;     // z index of that cell
 };
+constexpr int kSpanWords = sizeof(HoodSpan) / sizeof(int);
+static_assert(kMaxSpans * kSpanWords == kGroupSpanWords, "per-group span record size");
 
 __device__ __forceinline__ int hood_wrap(int a, int n) {
     a %= n;

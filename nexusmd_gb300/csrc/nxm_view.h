@@ -9,6 +9,9 @@
 
 namespace nxm {
 
+// ints per group of the saved neighbourhood span table (128 spans x 5 ints)
+constexpr int kGroupSpanWords = 640;
+
 struct CellGroup {
     int cell;   // first cell (global index)
     int ncell;  // consecutive cells along z in the group
@@ -45,6 +48,8 @@ struct DevView {
     struct CellGroup *groups;  // blocks of the tile kernels: runs of cells along z
     int ngroups;
     int hood_cap;        // capacity of a staged neighbourhood (atoms)
+    int *gspan;          // [ngroups][kGroupSpanWords]: each group's neighbourhood spans, written by the list build
+    int2 *gspan_n;       // [ngroups]: (atoms, spans) of that neighbourhood
     float4 *dtab;        // [S][kDtabStride] cell-image displacement per code
     double *xref;        // [3][N] positions at the last rebuild
     float4 *oref;        // mixed: cell offsets at the last rebuild, .w = q * sqrt(ke)
