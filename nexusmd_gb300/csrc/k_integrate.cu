@@ -23,35 +23,58 @@ __global__ void __launch_bounds__(256) k_integrate(DevView v, double dt, int rep
         Acc *ax = static_cast<Acc *>(v.fx) + s;
         Acc *ay = static_cast<Acc *>(v.fy) + s;
         Acc *az = static_cast<Acc *>(v.fz) + s;
-        double F[3] = {acc_value(*ax), acc_value(*ay), acc_value(*az)};
+        const Acc w[3] = {*ax, *ay, *az};
         *ax = (Acc)0;
         *ay = (Acc)0;
         *az = (Acc)0;
+        // forces in FP64 where they are needed (reports, FP64 update)
+        auto F = [&](int c) { return acc_value(w[c]); };
         double p[3] = {v.x[s], v.y[s], v.z[s]};
         double u[3] = {v.vx[s], v.vy[s], v.vz[s]};
         if (report) {
             int o = v.orig[s];
             double m = v.mass[s];
-            double w[3] = {u[0], u[1], u[2]};
+            double vh[3] = {u[0], u[1], u[2]};
             if (m > 0) {
                 double invMass = 1.0 / m;
                 double half = 0.5 * dt;
 #pragma unroll
-                for (int c = 0; c < 3; ++c) w[c] += F[c] * invMass * half;
+                for (int c = 0; c < 3; ++c) vh[c] += F(c) * invMass * half;
             }
-            ke = 0.5 * m * (w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+            ke = 0.5 * m * (vh[0] * vh[0] + vh[1] * vh[1] + vh[2] * vh[2]);
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 v.snap_x[3 * (size_t)o + c] = p[c];
                 v.snap_v[3 * (size_t)o + c] = u[c];
-                v.snap_f[3 * (size_t)o + c] = F[c];
+                v.snap_f[3 * (size_t)o + c] = F(c);
             }
         }
         double im = v.invm[s];
-        if (im != 0.0) {
+        if (im != 0.0 && v.mixed) {
+            // fixed-point forces: v += (invm dt 2^-32) * word, one multiply-add per
+            // component on the FP64 pipe (the order of the two scalings differs
+            // from the FP64 engine's only in the last bit)
+            const double c0 = im * (dt * kForceUnscale);
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                u[c] += im * F[c] * dt;
+                u[c] = fma(c0, (double)w[c], u[c]);
+                double q = fma(u[c], dt, p[c]);
+                if (q < S.lb[c])
+                    q += S.L[c];
+                else if (q > S.ub[c])
+                    q -= S.L[c];
+                p[c] = q;
+            }
+            v.x[s] = p[0];
+            v.y[s] = p[1];
+            v.z[s] = p[2];
+            v.vx[s] = u[0];
+            v.vy[s] = u[1];
+            v.vz[s] = u[2];
+        } else if (im != 0.0) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                u[c] += im * F(c) * dt;
                 double q = p[c] + u[c] * dt;
                 if (q < S.lb[c])
                     q += S.L[c];
@@ -92,7 +115,7 @@ __global__ void __launch_bounds__(256) k_integrate(DevView v, double dt, int rep
                 if (d2 > v.skin_half2) atomicOr(&v.flags->skin_hit, 1);
             }
             // FP64 accumulators can hold a non-finite sum; int64 ones cannot
-            if (!(isfinite(F[0]) && isfinite(F[1]) && isfinite(F[2]))) atomicOr(&v.flags->error, ERR_NONFINITE);
+            if (!(isfinite(F(0)) && isfinite(F(1)) && isfinite(F(2)))) atomicOr(&v.flags->error, ERR_NONFINITE);
         }
     }
     if (report) energy_add(v.E, sys, E_KIN, ke);
