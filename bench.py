@@ -333,7 +333,8 @@ def reporting(cfg, steps, interval, device):
     saved, null = os.dup(1), os.open(os.devnull, os.O_WRONLY)
     try:
         os.chdir(d)
-        for th, key in ((0, "sync_s"), (4, "async_s")):
+        # a short untimed run first (one-time costs), then each mode twice, best kept
+        for th, key in ((0, None), (0, "sync_s"), (4, "async_s"), (0, "sync_s"), (4, "async_s")):
             disp = NexusMD.TaskDispatcher.CreateDispatcher("GPU")
             disp.EnableHarmonicBondForce()
             disp.EnableHarmonicAngleForce()
@@ -344,10 +345,11 @@ def reporting(cfg, steps, interval, device):
             os.dup2(null, 1)  # Simulate prints a line per step
             t0 = time.perf_counter()
             try:
-                disp.Simulate(sp, st, pdb, "o%d.pdb" % th, DT_PS, steps, interval)
+                disp.Simulate(sp, st, pdb, "o%d.pdb" % th, DT_PS, steps if key else 2, interval)
             finally:
                 os.dup2(saved, 1)
-            out[key] = time.perf_counter() - t0
+            if key:
+                out[key] = min(out.get(key, 1e30), time.perf_counter() - t0)
             del disp
     finally:
         os.chdir(cwd)
@@ -461,7 +463,8 @@ def native(args):
             out["other_workloads"] = {
                 "c4": other_workload(4, 200, 10, local, check=not args.no_check),
                 "c5": other_workload(5, 100, 5, local, check=not args.no_check)}
-            out["simulate_reporting"] = [reporting(1, 400, 1, local), reporting(3, 100, 10, local)]
+            out["simulate_reporting"] = [reporting(1, 400, 1, local), reporting(3, 50, 1, local),
+                                         reporting(3, 100, 10, local)]
         if not args.no_cpu:
             out["cpu_baseline"] = cpu_baseline(s, steps=args.cpu_steps)
     if rank == 0:

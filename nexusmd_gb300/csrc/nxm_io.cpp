@@ -205,6 +205,13 @@ ParsedSystem parse_all(const std::string &system_xml, const std::string &state_x
 
 // ------------------------------------------------------------------ reports
 
+namespace {
+const char kDigitPairs[201] =
+    "00010203040506070809101112131415161718192021222324252627282930313233343536373839"
+    "40414243444546474849505152535455565758596061626364656667686970717273747576777879"
+    "8081828384858687888990919293949596979899";
+}  // namespace
+
 int fixed_chars(double x, int prec, int width, char *out) {
     static const unsigned long long p10[18] = {1ULL,
                                                10ULL,
@@ -226,42 +233,78 @@ int fixed_chars(double x, int prec, int width, char *out) {
                                                100000000000000000ULL};
     if (!(std::fabs(x) < 1099511627776.0) || prec < 0 || prec > 17 || width > 64)
         return std::min(std::snprintf(out, kFixedCharsMax, "%*.*f", width, prec, x), kFixedCharsMax - 1);
+    const bool neg = std::signbit(x);
+    // integer part and fraction, both exact: |x| < 2^40, so ip fits and
+    // |x| - ip is representable
+    const double ax = std::fabs(x);
+    unsigned long long ip = (unsigned long long)ax;
+    const double fr = ax - (double)ip;
+    // the fraction's exact value m * 2^-s scaled by 10^prec, rounded half to
+    // even on the whole number ip * 10^prec + fp (10^prec is even for prec > 0)
     unsigned long long bits;
-    std::memcpy(&bits, &x, sizeof bits);
-    const bool neg = (bits >> 63) != 0;
+    std::memcpy(&bits, &fr, sizeof bits);
     const int ex = (int)((bits >> 52) & 0x7ff);
     unsigned long long m = bits & ((1ULL << 52) - 1);
-    int s;  // |x| = m * 2^-s, s >= 12 below 2^40
+    int s;
     if (ex == 0) {
         s = 1074;
     } else {
         m |= 1ULL << 52;
-        s = 1075 - ex;
+        s = 1075 - ex;  // >= 53: fr < 1
     }
     using u128 = unsigned __int128;
     const u128 P = (u128)m * p10[prec];  // < 2^110
-    u128 N = 0;
+    unsigned long long fp = 0;
     if (s < 128) {
-        N = P >> s;
-        const u128 rem = P - (N << s), half = (u128)1 << (s - 1);
-        if (rem > half || (rem == half && (N & 1))) ++N;
-    }  // else P < 2^110 < half an ulp of the last place: rounds to zero
-    unsigned long long ip = (unsigned long long)(N / p10[prec]), fp = (unsigned long long)(N % p10[prec]);
+        const u128 q = P >> s;
+        const u128 rem = P - (q << s), half = (u128)1 << (s - 1);
+        fp = (unsigned long long)q;
+        const unsigned long long par = prec > 0 ? fp : fp + ip;
+        if (rem > half || (rem == half && (par & 1))) ++fp;
+        if (fp == p10[prec]) {  // rounded up to the next integer
+            fp = 0;
+            ++ip;
+        }
+    }  // else the fraction is below half an ulp of the last place: zero
+    // digits right to left into tmp[..64): the fraction as exactly prec
+    // digits, then the integer part; two digits per step, in 32-bit pieces
     char tmp[64];
-    int t = 0;
-    for (int d = 0; d < prec; ++d) {
-        tmp[t++] = (char)('0' + fp % 10);
-        fp /= 10;
+    char *e = tmp + 64, *p = e;
+    auto put8 = [&](unsigned v, int nd) {  // nd <= 8 digits of v (v < 10^nd)
+        for (; nd >= 2; nd -= 2) {
+            p -= 2;
+            std::memcpy(p, kDigitPairs + 2 * (v % 100), 2);
+            v /= 100;
+        }
+        if (nd) *--p = (char)('0' + v);
+    };
+    if (prec > 0) {
+        int nd = prec;
+        while (nd > 8) {
+            put8((unsigned)(fp % 100000000ULL), 8);
+            fp /= 100000000ULL;
+            nd -= 8;
+        }
+        put8((unsigned)fp, nd);
+        *--p = '.';
     }
-    if (prec > 0) tmp[t++] = '.';
-    do {
-        tmp[t++] = (char)('0' + ip % 10);
-        ip /= 10;
-    } while (ip);
-    if (neg) tmp[t++] = '-';
+    while (ip >= 100000000ULL) {
+        put8((unsigned)(ip % 100000000ULL), 8);
+        ip /= 100000000ULL;
+    }
+    {
+        unsigned v = (unsigned)ip;
+        do {
+            *--p = (char)('0' + v % 10);
+            v /= 10;
+        } while (v);
+    }
+    if (neg) *--p = '-';
+    const int t = (int)(e - p);
     int len = 0;
     for (int pad = width - t; pad > 0; --pad) out[len++] = ' ';
-    while (t) out[len++] = tmp[--t];
+    std::memcpy(out + len, p, t);
+    len += t;
     out[len] = 0;
     return len;
 }
@@ -449,7 +492,7 @@ bool ReportWriter::pvf(const double *pos, const double *vel, const double *frc, 
             buf.append(line, k);
         }
     };
-    int nt = std::max(1, std::min(threads, n / 4096 + 1));
+    int nt = std::max(1, std::min(threads, n / 1024 + 1));
     std::vector<std::string> parts(nt);
     if (nt == 1) {
         format(0, n, parts[0]);
