@@ -3,15 +3,16 @@
 erfc(x) = exp(-x^2) * g(x) with g = erfcx, the scaled complementary error
 function.  On x in [0, 4] (alpha*r up to 4 covers Ewald tolerances down to
 ~1e-7 at the cutoff) g is smooth in t = 1 / (1 + 0.4 x), t in [0.385, 1],
-so a degree-8 polynomial in t, least-squares fitted on Chebyshev nodes of t
-(a near-minimax fit), holds g to ~1e-8 relative in exact arithmetic and
-~3e-7 when evaluated by Horner's rule in FP32.  Run this file to print the
-coefficients pasted into nxm_common.cuh.
+so a degree-6 polynomial in t, least-squares fitted on Chebyshev nodes of t
+(a near-minimax fit), holds g to ~3e-7 relative in exact arithmetic and
+~5e-7 when evaluated by Horner's rule in FP32 (degree 8: 1e-8 and 2.5e-7,
+two more multiply-adds per pair for no gain that FP32 keeps).  Run this
+file to print the coefficients pasted into nxm_common.cuh.
 """
 import numpy as np
 from scipy.special import erfcx
 
-P, X, DEG = 0.4, 4.0, 8
+P, X, DEG = 0.4, 4.0, 6
 
 
 def fit():
