@@ -404,7 +404,8 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_pairs_mixed(DevView v) {
         const int cnt = v.ncount[i];
         const uint4 *lst4 = reinterpret_cast<const uint4 *>(v.nl16 + (size_t)i * v.stride) + lane;
         float fx = 0.f, fy = 0.f, fz = 0.f;
-        uint4 cur = cnt > 0 ? __ldg(lst4) : make_uint4(0, 0, 0, 0);
+        // the first chunk's slot always exists: its load need not wait for the count
+        uint4 cur = __ldg(lst4);
         for (int c0 = 0; c0 < cnt; c0 += 256) {
             // this lane's entries c0 + lane + 32u, u = 0..7, and the next chunk in flight
             uint4 nxt = c0 + 256 < cnt ? __ldg(lst4 + (c0 + 256) / 8) : make_uint4(0, 0, 0, 0);
