@@ -287,8 +287,9 @@ def batch_accuracy(systems, eng):
 
 
 def other_workload(cfg, steps, warmup, device, check=True):
-    """Throughput (and accuracy) of another named configuration: 4 = the
-    32-system uneven lambda-window batch in one context, 5 = ~474k atoms."""
+    """Throughput (and accuracy) of another named configuration: 1 = ~2,700
+    atoms, 2 = ~23,800 atoms, 4 = the 32-system uneven lambda-window batch in
+    one context, 5 = ~474k atoms."""
     import numpy as np
     from nexusmd_gb300 import synthetic as sy
     from nexusmd_gb300.engine import Engine
@@ -461,6 +462,8 @@ def native(args):
         if not args.quick:
             out["nve_drift"] = nve_drift(s, v0, kw)
             out["other_workloads"] = {
+                "c1": other_workload(1, 2000, 50, local, check=not args.no_check),
+                "c2": other_workload(2, 1000, 50, local, check=not args.no_check),
                 "c4": other_workload(4, 200, 10, local, check=not args.no_check),
                 "c5": other_workload(5, 100, 5, local, check=not args.no_check)}
             out["simulate_reporting"] = [reporting(1, 400, 1, local), reporting(3, 50, 1, local),

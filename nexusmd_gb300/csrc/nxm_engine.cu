@@ -333,18 +333,22 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         stride = std::max(stride, cap);
         // tile kernels: groups of G cells along z; the staged neighbourhood
         // holds 5 x 5 x (G + 4) cells.  The largest G whose neighbourhood
-        // (with 30% headroom over the mean density) stays within ~100 KB of
-        // shared memory, at most nz - 4 so no cell appears twice.
+        // (with 25% headroom over the mean density) holds at most 4,400
+        // atoms -- ~109 KB of shared memory per block, so two blocks of the
+        // pair kernel and of the list build share an SM -- and at most
+        // nz - 4, so no cell appears twice.  (Larger groups stage fewer
+        // atoms per atom of the group: at 94k atoms G = 3 runs the pair
+        // kernel 7% faster than G = 2.)
         double cell_atoms = sysd_[s].cs[0] * sysd_[s].cs[1] * sysd_[s].cs[2] * h.n / vol;
         int gmax = std::max(1, std::min(kMaxGroupCells, sysd_[s].nc[2] - 4));
         int G = 1;
         for (int g = gmax; g >= 1; --g)
-            if (25.0 * (g + 4) * cell_atoms * 1.3 + 128 <= 4200.0) {
+            if (25.0 * (g + 4) * cell_atoms * 1.25 + 128 <= 4400.0) {
                 G = g;
                 break;
             }
         group_g[s] = G;
-        int hood = (int)(25.0 * (G + 4) * cell_atoms * 1.3 + 128);
+        int hood = (int)(25.0 * (G + 4) * cell_atoms * 1.25 + 128);
         hood_cap = std::max(hood_cap, hood);
         off += h.n;
     }
