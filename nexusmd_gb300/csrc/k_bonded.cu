@@ -8,6 +8,7 @@
 // reference's single-shift minimum image; in mixed mode they are then
 // rounded to FP32 (the stiff bond terms cannot afford FP32 positions) and the
 // rest of the term is FP32 with int64 fixed-point force accumulation.
+#include "nxm_pairterms.cuh"
 #include "nxm_view.h"
 
 namespace nxm {
@@ -88,12 +89,24 @@ __device__ __forceinline__ V3<R> normalized(const V3<R> &a) {
     return mk<R>(0, 0, 0);
 }
 
+// One thread per term over [bonds | angles | torsions], followed, when
+// `pairs` is set, by [excluded pairs | exception pairs] (nxm_pairterms.cuh):
+// every per-term force of a step in one launch.
 template <typename R, typename Acc>
-__global__ void __launch_bounds__(256) k_bonded(DevView v, int energy) {
+__global__ void __launch_bounds__(256) k_bonded(DevView v, int energy, int pairs) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
-    int total = v.nb + v.na + v.nt;
+    const int nbt = v.nb + v.na + v.nt;
+    const int nx = pairs ? v.nex : 0, nc = pairs ? v.nxc : 0;
+    int total = nbt;
     double e = 0.0;
     int term = -1, sys = 0;
+    if (t >= nbt && t < nbt + nx) {
+        term = E_EXCL;
+        e = exclusion_pair<sizeof(R) == 4>(v, t - nbt, sys);
+    } else if (t >= nbt + nx && t < nbt + nx + nc) {
+        term = E_EXCEPT;
+        e = exception_pair<sizeof(R) == 4>(v, t - nbt - nx, sys);
+    }
     if (t < total) {
         if (t < v.nb) {
             // HarmonicBondForce.cpp:20-58
@@ -183,19 +196,26 @@ __global__ void __launch_bounds__(256) k_bonded(DevView v, int energy) {
         }
     }
     if (energy) {
-        // three energy terms: reduce each separately (all lanes participate)
+        // each energy term reduced separately (all lanes participate)
         for (int k = E_BOND; k <= E_TORSION; ++k) energy_add(v.E, sys, k, term == k ? e : 0.0);
+        if (pairs) {
+            energy_add(v.E, sys, E_EXCL, term == E_EXCL ? e : 0.0);
+            energy_add(v.E, sys, E_EXCEPT, term == E_EXCEPT ? e : 0.0);
+        }
     }
 }
 
-void launch_bonded(const DevView &v, int energy, cudaStream_t st) {
-    int n = v.nb + v.na + v.nt;  // disabled kinds arrive with a zero count
-    if (n == 0) return;
+// pairs != 0: the exclusion correction and the exception pairs too (the
+// caller passes it only when the nonbonded force is on)
+int launch_bonded(const DevView &v, int energy, cudaStream_t st, int pairs) {
+    int n = v.nb + v.na + v.nt + (pairs ? v.nex + v.nxc : 0);  // disabled kinds arrive with a zero count
+    if (n == 0) return 0;
     int nb = (n + 255) / 256;
     if (v.mixed)
-        k_bonded<float, long long><<<nb, 256, 0, st>>>(v, energy);
+        k_bonded<float, long long><<<nb, 256, 0, st>>>(v, energy, pairs);
     else
-        k_bonded<double, double><<<nb, 256, 0, st>>>(v, energy);
+        k_bonded<double, double><<<nb, 256, 0, st>>>(v, energy, pairs);
+    return 1;
 }
 
 }  // namespace nxm

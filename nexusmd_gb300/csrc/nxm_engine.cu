@@ -793,8 +793,9 @@ std::string Engine::set_velocities(const double *xyz) {
 // Force kernels of one evaluation (everything but the integrator).
 // Kernel launches of force_launches below, without launching.
 static int force_launch_count(const DevView &v) {
-    int n = (v.nb + v.na + v.nt) ? 1 : 0;
-    if (v.force_mask & NXM_FORCE_NONBONDED) n += 1 + (v.nex ? 1 : 0) + (v.nxc ? 1 : 0) + 7;
+    bool nb = (v.force_mask & NXM_FORCE_NONBONDED) != 0;
+    int n = (v.nb + v.na + v.nt + (nb ? v.nex + v.nxc : 0)) ? 1 : 0;
+    if (nb) n += 1 + 7;
     return n;
 }
 
@@ -811,21 +812,11 @@ static int force_launches(const DevView &v, const FftPlan &plan, int energy, cud
         launch_pme(v, plan, energy, pme_st);
         n += 7;
     }
-    if (v.nb + v.na + v.nt) {
-        launch_bonded(v, energy, st);
-        ++n;
-    }
+    // bonded terms, exclusion correction and exceptions: one launch
+    n += launch_bonded(v, energy, st, nb ? 1 : 0);
     if (nb) {
         launch_pairs(v, energy, st);
         ++n;
-        if (v.nex) {
-            launch_exclusions(v, energy, st);
-            ++n;
-        }
-        if (v.nxc) {
-            launch_exceptions(v, energy, st);
-            ++n;
-        }
         if (!pme_st) {
             launch_pme(v, plan, energy, st);
             n += 7;

@@ -93,7 +93,9 @@ void launch_nlist_rebuild(const DevView &v, cudaStream_t st);
 void launch_build(const DevView &v, cudaStream_t st);
 void tiles_set_smem(int hood_cap);
 void launch_derive_inputs(const DevView &v, cudaStream_t st);
-void launch_bonded(const DevView &v, int energy, cudaStream_t st);
+// bonded terms; with pairs != 0 also the exclusion correction and the
+// exception pairs, in the same launch.  Returns the number of launches (0, 1).
+int launch_bonded(const DevView &v, int energy, cudaStream_t st, int pairs = 0);
 void launch_pairs(const DevView &v, int energy, cudaStream_t st);
 void launch_exclusions(const DevView &v, int energy, cudaStream_t st);
 void launch_exceptions(const DevView &v, int energy, cudaStream_t st);
