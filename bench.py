@@ -72,6 +72,12 @@ def init_pg(ws):
     return dist
 
 
+def replica_throughput(world, atoms, steps, seconds):
+    """Whole-job atom-steps/s of `world` independent replicas of `atoms`
+    atoms, each running `steps` steps, timed by the slowest rank."""
+    return world * atoms * steps / seconds
+
+
 def barrier(dist):
     if dist is not None:
         dist.barrier()
@@ -383,7 +389,7 @@ def native(args):
     rebuilds = eng.rebuilds() - rb0
     launches, rb_launches = eng.launches_per_step()
     per_step = ms / args.steps
-    value = ws * s.n * args.steps / (ms * 1e-3)
+    value = replica_throughput(ws, s.n, args.steps, ms * 1e-3)
 
     # end to end through the C ABI from host arrays: context creation and
     # upload, then per step one nxm_step(1) call and a read-back of the
@@ -417,7 +423,7 @@ def native(args):
                                              "pme_threads_per_block"), eng.tuning())),
                       "replicas": ws, "l2": "inputs larger than L2 (neighbour list %.0f MB per step)"
                                           % (s.n * 560 * 2 / 1e6)},
-           "e2e": {"value": ws * s.n * args.steps / e2e_s, "unit": "atom-steps/s",
+           "e2e": {"value": replica_throughput(ws, s.n, args.steps, e2e_s), "unit": "atom-steps/s",
                    "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h},
            # per step: the step's kernels (one graph launch); per list rebuild: the rebuild kernels
            "gpu_launches": launches * args.steps + rb_launches * rebuilds,
