@@ -227,13 +227,15 @@ __global__ void __launch_bounds__(256) k_gather(DevView v, const FftSysDev *fs) 
     acc_add(static_cast<Acc_ *>(v.fz) + s, -(q * (fz * (R)(F.K[2] * S.invL[2]))));
 }
 
-// Per-atom spread: bound by the throughput of the 125 int64 L2 atomics per
-// atom (60 us for 94,100 atoms).  Two alternatives were measured slower on
-// that system and dropped: one block per 8x8x8 grid tile summing its points
-// in shared memory with no global atomics (64 us: the search for the atoms
-// that reach a tile costs ~155 instructions per contribution), and one
-// block per box of cells with a shared-memory sub-grid flushed by one
-// atomic per point (88 us: too few blocks for the serial per-atom loops).
+// Spread: bound by the L2 atomics (125 int64 per atom), and by how many
+// memory sectors each atomic instruction touches -- hence the warp-per-atom
+// layout in mixed mode (the FP64 engine keeps one atom per thread).
+// Alternatives measured slower at 94,100 atoms and dropped: one block per
+// 8x8x8 grid tile summing its points in shared memory with no global
+// atomics (the search for the atoms that reach a tile costs ~155
+// instructions per contribution), a shared-memory sub-grid per box of cells
+// or per 32-slot clump flushed by one atomic per point (fewer global
+// atomics, no faster), and five threads per atom (one x-plane each).
 void launch_spread(const DevView &v, const FftPlan &plan, cudaStream_t st) {
     // the accumulator (int64 fixed point or double, 8 bytes per point) starts at zero
     cudaMemsetAsync(v.grid_acc, 0, sizeof(long long) * (size_t)v.total_grid, st);
