@@ -150,21 +150,37 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_warp(DevView v, co
         s_i[warp][lane][3] = sys;
     }
     __syncwarp();
+    const unsigned full = 0xffffffffu;
     for (int a = 0; a < 32; ++a) {
         const int sys = s_i[warp][a][3];
         if (sys < 0) continue;
         const FftSysDev &F = fs[sys];
         const int K0 = F.K[0], K1 = F.K[1], K2 = F.K[2];
-        long long *g = static_cast<long long *>(v.grid_acc) + F.roff;
+        unsigned long long *g = reinterpret_cast<unsigned long long *>(static_cast<long long *>(v.grid_acc) + F.roff);
         const float *w = s_w[warp][a];
-        const int x0 = s_i[warp][a][0], y0 = s_i[warp][a][1], z0 = s_i[warp][a][2];
-        for (int p = lane; p < 125; p += 32) {
-            const int ix = p / 25, r = p - 25 * ix, iy = r / 5, iz = r - 5 * iy;
-            int xi = x0 + ix, yi = y0 + iy, zi = z0 + iz;
+        // lane r < 25: grid row (ix, iy) = (r / 5, r % 5) of the atom, its
+        // offset and its weight (q wx) wy
+        long long row_off = 0;
+        float row_w = 0.f;
+        if (lane < 25) {
+            const int ix = lane / 5, iy = lane - 5 * ix;
+            int xi = s_i[warp][a][0] + ix, yi = s_i[warp][a][1] + iy;
             xi -= xi >= K0 ? K0 : 0;
             yi -= yi >= K1 ? K1 : 0;
+            row_off = ((long long)xi * K1 + yi) * K2;
+            row_w = w[15] * w[ix] * w[5 + iy];
+        }
+        const int z0 = s_i[warp][a][2];
+        // point p = 5 row + iz: 32 consecutive points per instruction
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int p = lane + 32 * k;
+            const int row = min(p / 5, 24), iz = p - 5 * row;
+            const long long off = __shfl_sync(full, row_off, row);
+            const float rw = __shfl_sync(full, row_w, row);
+            int zi = z0 + iz;
             zi -= zi >= K2 ? K2 : 0;
-            grid_add(g + ((long long)xi * K1 + yi) * K2 + zi, w[15] * w[ix] * w[5 + iy] * w[10 + iz]);
+            if (p < 125) atomicAdd(g + off + zi, to_fixed32(rw * w[10 + iz]));
         }
     }
 }
