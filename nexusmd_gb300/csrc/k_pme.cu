@@ -101,20 +101,22 @@ __global__ void __launch_bounds__(256) k_spread(DevView v, const FftSysDev *fs) 
 }
 
 // Mixed-precision spread with the warp's lanes on one atom's points: each
-// lane first prepares one atom of the warp (grid index, fraction, weights),
-// then the warp walks its 32 atoms and spreads each atom's 125 points with
-// 32 consecutive points per instruction.  Consecutive points share grid
-// rows (5 contiguous words per row), so one atomic instruction touches ~13
-// memory sectors instead of the 32 of one-atom-per-lane.  The values are
-// the per-atom kernel's ((q wx) wy) wz, so the grid is identical.
-constexpr int kSpreadWarps = 8;
+// of the first kSpreadAtoms lanes prepares one atom of the warp (grid index,
+// fraction, weights), then the warp walks those atoms and spreads each
+// atom's 125 points with 32 consecutive points per instruction.
+// Consecutive points share grid rows (5 contiguous words per row), so one
+// atomic instruction touches ~13 memory sectors instead of the 32 of
+// one-atom-per-lane; 16 atoms per warp keep twice as many warps in flight as
+// 32 would.  The values are the per-atom kernel's ((q wx) wy) wz, so the
+// grid is identical.
+constexpr int kSpreadWarps = 8, kSpreadAtoms = 16;  // atoms per warp
 
 __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_warp(DevView v, const FftSysDev *fs) {
-    __shared__ float s_w[kSpreadWarps][32][16];  // wx[5] wy[5] wz[5] q
-    __shared__ int s_i[kSpreadWarps][32][4];     // grid index x y z, system (-1: none)
+    __shared__ float s_w[kSpreadWarps][kSpreadAtoms][16];  // wx[5] wy[5] wz[5] q
+    __shared__ int s_i[kSpreadWarps][kSpreadAtoms][4];     // grid index x y z, system (-1: none)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int s = (blockIdx.x * kSpreadWarps + warp) * 32 + lane;
-    {
+    const int s = (blockIdx.x * kSpreadWarps + warp) * kSpreadAtoms + lane;
+    if (lane < kSpreadAtoms) {
         int sys = -1;
         if (s < v.N) {
             sys = v.sys_of[s];
@@ -151,7 +153,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_warp(DevView v, co
     }
     __syncwarp();
     const unsigned full = 0xffffffffu;
-    for (int a = 0; a < 32; ++a) {
+    for (int a = 0; a < kSpreadAtoms; ++a) {
         const int sys = s_i[warp][a][3];
         if (sys < 0) continue;
         const FftSysDev &F = fs[sys];
@@ -175,7 +177,7 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_warp(DevView v, co
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const int p = lane + 32 * k;
-            const int row = min(p / 5, 24), iz = p - 5 * row;
+            const int row = min(p / 5, 24), iz = min(p - 5 * row, 4);  // (clamped past point 124)
             const long long off = __shfl_sync(full, row_off, row);
             const float rw = __shfl_sync(full, row_w, row);
             int zi = z0 + iz;
@@ -257,7 +259,8 @@ void launch_spread(const DevView &v, const FftPlan &plan, cudaStream_t st) {
     cudaMemsetAsync(v.grid_acc, 0, sizeof(long long) * (size_t)v.total_grid, st);
     int t = v.pme_block, nb = (v.N + t - 1) / t;
     if (v.mixed)
-        k_spread_warp<<<(v.N + kSpreadWarps * 32 - 1) / (kSpreadWarps * 32), kSpreadWarps * 32, 0, st>>>(v, plan.dsys);
+        k_spread_warp<<<(v.N + kSpreadWarps * kSpreadAtoms - 1) / (kSpreadWarps * kSpreadAtoms), kSpreadWarps * 32, 0,
+                        st>>>(v, plan.dsys);
     else
         k_spread<double, double><<<nb, t, 0, st>>>(v, plan.dsys);
 }
