@@ -399,7 +399,9 @@ def native(args):
     t0 = time.perf_counter()
     eng2 = Engine(s, precision=1, **kw)
     eng2.set_velocities(v0)
-    frame = np.zeros((s.n, 3))
+    # the position frame lands in pinned host memory
+    import torch
+    frame = torch.zeros((s.n, 3), dtype=torch.float64, pin_memory=True).numpy()
     en = Energies()
     for _ in range(args.steps):
         eng2.step(1, DT_PS)
