@@ -423,7 +423,8 @@ def native(args):
                       "rebuild_interval": 10, "dt_fs": DT_PS * 1000, "precision": "mixed",
                       "v0": "Maxwell-Boltzmann 300 K", "list_rebuilds_in_timed_steps": rebuilds,
                       "autotuned": dict(zip(("fft_lines_per_z_block", "fft_cols_per_yx_block",
-                                             "pme_threads_per_block"), eng.tuning())),
+                                             "pme_threads_per_block"), eng.tuning()),
+                                        fft_plane_threads=eng.fft_plane_threads()),
                       "replicas": ws, "l2": "inputs larger than L2 (neighbour list %.0f MB per step)"
                                           % (s.n * 560 * 2 / 1e6)},
            "e2e": {"value": replica_throughput(ws, s.n, args.steps, e2e_s), "unit": "atom-steps/s",

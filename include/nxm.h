@@ -104,6 +104,12 @@ typedef struct {
     int32_t state_velocities; /* Simulate only: 1 = start from the state XML's <Velocities>
                                  when it has one per atom; 0 (default) = zero velocities,
                                  as the reference */
+    int32_t fft_lines;        /* 0 (default): the PME FFT runs on the plane path (one block
+                                 per x-plane for the z and y transforms, 3 launches) when
+                                 every plane fits in shared memory; 1 = always the line
+                                 path (5 launches).  The same arithmetic: bit-equal results
+                                 when K1 is even; with odd K1 the z transforms pair other
+                                 lines, which changes only the rounding. */
 } nxm_options;
 
 /* Energies of one system (kJ/mol) at the last evaluation that computed them. */
@@ -178,10 +184,15 @@ int nxm_profile_phases(nxm_ctx *ctx, int32_t nsteps, double dt, double *ms, int3
  * decides (list age or displacement beyond half the skin). */
 int nxm_rebuild_count(nxm_ctx *ctx, int64_t *count);
 
-/* Launch shapes in use: [0] FFT real lines per z-pass block, [1] FFT
- * columns per y/x-pass block, [2] threads per spread/gather block (the
- * autotuner's picks, or the defaults 16, 8, 128). */
+/* Launch shapes in use: [0] FFT real lines per z-pass block, or 0 when the
+ * FFT runs on the plane path (one block per x-plane for the z and y
+ * transforms), [1] FFT columns per x-pass (and y-pass) block, [2] threads per
+ * spread/gather block (the autotuner's picks, or the defaults). */
 int nxm_get_tuning(nxm_ctx *ctx, int32_t out[3]);
+
+/* Threads per block of the FFT's plane path (the autotuner's pick or the
+ * default), or 0 when the FFT runs on the line path. */
+int nxm_get_fft_plane_threads(nxm_ctx *ctx, int32_t *threads);
 
 /* Kernel launches one step issues (steady state, no list rebuild). */
 int nxm_launches_per_step(nxm_ctx *ctx, int32_t *launches, int32_t *rebuild_launches);

@@ -10,6 +10,17 @@
 // convolution with the influence function and the reciprocal energy sum
 // (NonbondedForce.cpp:323-388) are fused into the x pass between its forward
 // and inverse transforms, so the spectrum never makes an extra trip to memory.
+//
+// Two launch shapes with the same arithmetic (bit for bit):
+//  * plane path (3 kernels): one block per x-plane does the z transforms and
+//    then the y transforms of that plane in shared memory (forward), the x
+//    kernel convolves, one block per x-plane does y and then z (inverse);
+//  * line path (5 kernels): z, y, x, y, z, each kernel over tiles of lines --
+//    for planes too large for shared memory, and for the no-allocation entry.
+// Every pass has its radix fixed at compile time and reads its twiddles from
+// a shared-memory copy of the axis's table; lines in shared memory have an odd
+// stride (in complex words) so that column accesses do not conflict on banks.
+#include <algorithm>
 #include <mutex>
 
 #include "nxm_fft.h"
@@ -43,8 +54,8 @@ template <typename C>
 __device__ __forceinline__ C cscale(C a, typename Cx<C>::R s) { return Cx<C>::mk(a.x * s, a.y * s); }
 
 // Length-R DFT with root exp(sign * 2 pi i / R), R in {2, 3, 4, 5}.
-template <typename C>
-__device__ __forceinline__ void small_dft(C *v, int R, typename Cx<C>::R s) {
+template <typename C, int R>
+__device__ __forceinline__ void small_dft(C *v, typename Cx<C>::R s) {
     using T = typename Cx<C>::R;
     if (R == 2) {
         C a = v[0], b = v[1];
@@ -87,53 +98,102 @@ __device__ __forceinline__ void small_dft(C *v, int R, typename Cx<C>::R s) {
 // float rounding of the product.
 __device__ __forceinline__ int quot(int a, float inv_d) { return (int)(((float)a + 0.5f) * inv_d); }
 
-// Transform `nlines` contiguous lines of length n held in a (scratch b);
-// returns the buffer that holds the result.  Stockham pass with radix R after
-// sub-transforms of size Ns: element j + r*n/R, twiddled by
-// W_n^(r (j mod Ns) n/(Ns R)), goes to (j div Ns) Ns R + (j mod Ns) + r Ns.
-template <typename C>
-__device__ C *fft_lines(C *a, C *b, int n, int nlines, const int *rad, int np, const C *tw,
-                        int sign) {
+// One Stockham pass of radix R after sub-transforms of size Ns, over nl
+// lines of length n; line l of the source starts at src + l*lds, of the
+// destination at dst + l*ldd.  Butterfly j (n/R per line) takes the
+// elements j + r n/R, twiddles them by W_n^(r (j mod Ns) n/(Ns R)) (`tw`
+// holds W_n^t = exp(-2 pi i t / n); conjugated for the inverse), and writes
+// (j div Ns) Ns R + (j mod Ns) + r Ns.
+template <typename C, int R, bool INV>
+__device__ __forceinline__ void stockham(const C *src, int lds, C *dst, int ldd, int n, int nl, int Ns,
+                                         const C *tw) {
     using T = typename Cx<C>::R;
-    int Ns = 1;
-    for (int p = 0; p < np; ++p) {
-        int R = rad[p];
-        int m = n / R;
-        int step = n / (Ns * R);
-        int tot = nlines * m;
-        const float inv_m = 1.0f / (float)m, inv_ns = 1.0f / (float)Ns;
-        for (int bi = threadIdx.x; bi < tot; bi += blockDim.x) {
-            int l = quot(bi, inv_m), j = bi - l * m;
-            const C *src = a + l * n;
-            C *dst = b + l * n;
-            int jq = quot(j, inv_ns);
-            int k = j - jq * Ns;
-            C v[5];
+    const int m = n / R, step = n / (Ns * R), tot = nl * m;
+    const float inv_m = 1.0f / (float)m, inv_ns = 1.0f / (float)Ns;
+    for (int bi = threadIdx.x; bi < tot; bi += blockDim.x) {
+        int l = quot(bi, inv_m), j = bi - l * m;
+        int jq = quot(j, inv_ns), k = j - jq * Ns;
+        const C *s = src + l * lds + j;
+        C v[5];
 #pragma unroll
-            for (int r = 0; r < 5; ++r)
-                if (r < R) v[r] = src[j + r * m];
+        for (int r = 0; r < R; ++r) v[r] = s[r * m];
+        if (k) {
 #pragma unroll
-            for (int r = 1; r < 5; ++r) {
-                if (r < R && k) {
-                    C w = tw[r * k * step];
-                    if (sign > 0) w.y = -w.y;
-                    v[r] = cmul(v[r], w);
-                }
+            for (int r = 1; r < R; ++r) {
+                C w = tw[r * k * step];
+                if (INV) w.y = -w.y;
+                v[r] = cmul(v[r], w);
             }
-            small_dft(v, R, (T)sign);
-            int idx = jq * Ns * R + k;
+        }
+        small_dft<C, R>(v, (T)(INV ? 1 : -1));
+        C *d = dst + l * ldd + jq * Ns * R + k;
 #pragma unroll
-            for (int r = 0; r < 5; ++r)
-                if (r < R) dst[idx + r * Ns] = v[r];
+        for (int r = 0; r < R; ++r) d[r * Ns] = v[r];
+    }
+}
+
+// All passes of one axis over nl lines of length n.  Pass 0 reads `in`
+// (line stride ldi); the passes then alternate between the scratch buffers
+// s0 and s1 (stride lds), s0 first; the last pass writes `out` (stride ldo)
+// when it is given.  `in` must not be s0; it may be s1 (it is dead after
+// pass 0) and it may be `out` (a single pass then goes through s0 and is
+// copied).  Returns the buffer holding the result and sets *ldr to its line
+// stride.  Ends with a barrier.
+template <typename C, bool INV>
+__device__ C *line_fft(C *in, int ldi, C *out, int ldo, C *s0, C *s1, int lds, int n, int nl, const int *rad,
+                       int np, const C *tw, int *ldr) {
+    C *src = in;
+    int ls = ldi, Ns = 1;
+    for (int p = 0; p < np; ++p) {
+        C *dst = (p & 1) ? s1 : s0;
+        int ld = lds;
+        if (out && p == np - 1 && !(p == 0 && out == in)) {
+            dst = out;
+            ld = ldo;
+        }
+        switch (rad[p]) {
+            case 4: stockham<C, 4, INV>(src, ls, dst, ld, n, nl, Ns, tw); break;
+            case 2: stockham<C, 2, INV>(src, ls, dst, ld, n, nl, Ns, tw); break;
+            case 3: stockham<C, 3, INV>(src, ls, dst, ld, n, nl, Ns, tw); break;
+            default: stockham<C, 5, INV>(src, ls, dst, ld, n, nl, Ns, tw); break;
         }
         __syncthreads();
-        C *t = a;
-        a = b;
-        b = t;
-        Ns *= R;
+        src = dst;
+        ls = ld;
+        Ns *= rad[p];
     }
-    return a;
+    if (out && src != out) {
+        const float inv_n = 1.0f / (float)n;
+        for (int e = threadIdx.x; e < nl * n; e += blockDim.x) {
+            int l = quot(e, inv_n), i = e - l * n;
+            out[l * ldo + i] = src[l * ls + i];
+        }
+        __syncthreads();
+        src = out;
+        ls = ldo;
+    }
+    *ldr = ls;
+    return src;
 }
+
+// Moves `total` elements, U per thread per round: the U loads of a round
+// are all issued before the first is used, so a thread waits for one memory
+// latency per round instead of one per element.  load(e) must be valid for
+// every e < total (a round's tail reloads element total - 1); store(e, value)
+// runs for e < total only.
+template <int U, typename Load, typename Store>
+__device__ __forceinline__ void rounds(int total, Load load, Store store) {
+    const int bd = blockDim.x;
+    for (int e0 = threadIdx.x; e0 < total; e0 += U * bd) {
+        decltype(load(0)) val[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) val[u] = load(min(e0 + u * bd, total - 1));
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (e0 + u * bd < total) store(e0 + u * bd, val[u]);
+    }
+}
+constexpr int kRounds = 4;
 
 // Fixed-point grid word (units of 2^-32) to float without the FP64 pipe:
 // g = hi * 2^24 + lo with lo in [0, 2^24) splits it into two floats that are
@@ -146,171 +206,331 @@ __device__ __forceinline__ float grid_value(long long g) {
 }
 __device__ __forceinline__ double grid_value(double g) { return g; }
 
+// Copies the twiddle table of length n at `off` into shared memory (the
+// caller's next barrier publishes it).
 template <typename C>
-__device__ __forceinline__ const C *tw_table(const DevView &v, int off) {
-    return static_cast<const C *>(v.twiddle) + off;
+__device__ __forceinline__ void load_tw(C *dst, const DevView &v, int off, int n) {
+    const C *src = static_cast<const C *>(v.twiddle) + off;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
 }
 
-// ---- z: real -> half spectrum.  Reads the spread accumulator (fixed point
-// in mixed mode; the spread launch clears it first).  Two real lines go through
-// one complex transform (line 2p as the real part, 2p+1 as the imaginary
-// part) and are separated with X_a[k] = (Z[k] + conj Z[n-k]) / 2,
-// X_b[k] = (Z[k] - conj Z[n-k]) / 2i.
+// ---- z forward on nc real line pairs: line pair p (real lines ya = 2p and
+// ya + 1 of `acc`, row length K2; the second may not exist) becomes one
+// complex line, and after the transform they are separated with
+// X_a[k] = (Z[k] + conj Z[n-k]) / 2, X_b[k] = (Z[k] - conj Z[n-k]) / 2i.
+// `put(p, k, Xa, Xb, has_b)` stores the half spectra.
+template <typename C, typename Acc, typename Put>
+__device__ __forceinline__ void z_forward(const Acc *acc, int nreal, int nc, int n, int Kh, C *a, C *b, int ld,
+                                          const FftSysDev &F, const C *tw, Put put) {
+    using T = typename Cx<C>::R;
+    const float inv_n = 1.0f / (float)n, inv_kh = 1.0f / (float)Kh;
+    rounds<kRounds>(
+        nc * n,
+        [&](int e) {
+            int p = quot(e, inv_n), z = e - p * n;
+            int la = 2 * p, lb = min(la + 1, nreal - 1);
+            Acc ga = __ldcs(acc + (long long)la * n + z);
+            Acc gb = __ldcs(acc + (long long)lb * n + z);
+            return Cx<C>::mk((T)grid_value(ga), la + 1 < nreal ? (T)grid_value(gb) : (T)0);
+        },
+        [&](int e, C val) {
+            int p = quot(e, inv_n);
+            a[p * ld + e - p * n] = val;
+        });
+    __syncthreads();
+    int ldr;
+    C *res = line_fft<C, false>(a, ld, nullptr, 0, b, a, ld, n, nc, F.rad[2], F.np[2], tw, &ldr);
+    for (int e = threadIdx.x; e < nc * Kh; e += blockDim.x) {
+        int p = quot(e, inv_kh), k = e - p * Kh;
+        C z = res[p * ldr + k];
+        C zc = res[p * ldr + (k == 0 ? 0 : n - k)];
+        put(p, k, Cx<C>::mk((T)0.5 * (z.x + zc.x), (T)0.5 * (z.y - zc.y)),
+            Cx<C>::mk((T)0.5 * (z.y + zc.y), (T)0.5 * (zc.x - z.x)), 2 * p + 1 < nreal);
+    }
+    __syncthreads();
+}
+
+// ---- z inverse on nc line pairs: the Hermitian lines A = get(p, kk, 0) and
+// B = get(p, kk, 1) (kk <= n/2, completed by conjugation above) are combined
+// as Z = A + iB; the real and imaginary parts of the inverse transform are
+// the real output lines 2p and 2p + 1 of `out` (row length n).
+template <typename C, typename Get>
+__device__ __forceinline__ void z_inverse(typename Cx<C>::R *out, int nreal, int nc, int n, int Kh, C *a, C *b, int ld,
+                                          const FftSysDev &F, const C *tw, Get get) {
+    using T = typename Cx<C>::R;
+    const float inv_n = 1.0f / (float)n;
+    rounds<kRounds>(
+        nc * n,
+        [&](int e) {
+            int p = quot(e, inv_n), k = e - p * n;
+            bool upper = k >= Kh;
+            int kk = upper ? n - k : k;
+            C A = get(p, kk, 0);
+            C B = get(p, kk, 2 * p + 1 < nreal ? 1 : 0);
+            if (2 * p + 1 >= nreal) B = Cx<C>::mk((T)0, (T)0);
+            if (upper) {
+                A.y = -A.y;
+                B.y = -B.y;
+            }
+            return Cx<C>::mk(A.x - B.y, A.y + B.x);
+        },
+        [&](int e, C val) {
+            int p = quot(e, inv_n);
+            a[p * ld + e - p * n] = val;
+        });
+    __syncthreads();
+    int ldr;
+    C *res = line_fft<C, true>(a, ld, nullptr, 0, b, a, ld, n, nc, F.rad[2], F.np[2], tw, &ldr);
+    for (int e = threadIdx.x; e < nc * n; e += blockDim.x) {
+        int p = quot(e, inv_n), z = e - p * n;
+        C r = res[p * ldr + z];
+        out[(long long)(2 * p) * n + z] = r.x;
+        if (2 * p + 1 < nreal) out[(long long)(2 * p + 1) * n + z] = r.y;
+    }
+    __syncthreads();
+}
+
+// ================= plane path: one block per (system, x) =================
+// Shared memory: twiddles of y and z (twcap), the plane Q as Kh columns of
+// length K1 with odd stride ldq (qcap), two scratch buffers of `scr` words.
+
 template <typename C, typename Acc>
-__global__ void k_fft_z_fwd(DevView v, const FftSysDev *fs, const FftWork *work, int L) {
-    using T = typename Cx<C>::R;
+__global__ void __launch_bounds__(1024) k_fft_plane_fwd(DevView v, const FftSysDev *fs, const FftWork *work,
+                                                        int twcap, int qcap, int scr) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    C *a = reinterpret_cast<C *>(smem_raw);
+    C *twy = reinterpret_cast<C *>(smem_raw);
     FftWork w = work[blockIdx.x];
     const FftSysDev &F = fs[w.sys];
-    int n = F.K[2], Kh = F.Kh;
-    int nl_total = F.K[0] * F.K[1];
-    int l0 = w.unit * L;
-    int nl = min(L, nl_total - l0);
-    int np2 = (nl + 1) >> 1;  // complex lines
-    C *b = a + (L >> 1) * n;
-    const Acc *acc = static_cast<const Acc *>(v.grid_acc) + F.roff + (long long)l0 * n;
-    for (int e = threadIdx.x; e < np2 * n; e += blockDim.x) {
-        int p = e / n, z = e - p * n;
-        int la = 2 * p, lb = 2 * p + 1;
-        Acc ga = __ldcs(acc + (long long)la * n + z);
-        Acc gb = lb < nl ? __ldcs(acc + (long long)lb * n + z) : (Acc)0;
-        a[e] = Cx<C>::mk((T)grid_value(ga), (T)grid_value(gb));
+    const int K1 = F.K[1], K2 = F.K[2], Kh = F.Kh, x = w.unit;
+    const int ldq = K1 | 1, ldz = K2 | 1;
+    C *twz = twy + K1;
+    C *Q = twy + twcap;
+    C *A = Q + qcap;
+    C *B = A + scr;
+    load_tw(twy, v, F.tw[1], K1);
+    load_tw(twz, v, F.tw[2], K2);
+    const Acc *acc = static_cast<const Acc *>(v.grid_acc) + F.roff + (long long)x * K1 * K2;
+    const int npairs = (K1 + 1) >> 1, zc = min(npairs, scr / ldz);
+    for (int p0 = 0; p0 < npairs; p0 += zc) {
+        const int nc = min(zc, npairs - p0), y0 = 2 * p0;
+        z_forward<C, Acc>(acc + (long long)y0 * K2, K1 - y0, nc, K2, Kh, A, B, ldz, F, twz,
+                          [&](int p, int k, C xa, C xb, bool hb) {
+                              Q[k * ldq + y0 + 2 * p] = xa;
+                              if (hb) Q[k * ldq + y0 + 2 * p + 1] = xb;
+                          });
     }
-    __syncthreads();
-    C *res = fft_lines(a, b, n, np2, F.rad[2], F.np[2], tw_table<C>(v, F.tw[2]), -1);
-    C *out = static_cast<C *>(v.grid_cplx) + F.coff + (long long)l0 * Kh;
-    for (int e = threadIdx.x; e < np2 * Kh; e += blockDim.x) {
-        int p = e / Kh, k = e - p * Kh;
-        C z = res[p * n + k];
-        C zc = res[p * n + (k == 0 ? 0 : n - k)];
-        // A = (z + conj zc)/2, B = (z - conj zc)/(2i)
-        out[(long long)(2 * p) * Kh + k] = Cx<C>::mk((T)0.5 * (z.x + zc.x), (T)0.5 * (z.y - zc.y));
-        if (2 * p + 1 < nl)
-            out[(long long)(2 * p + 1) * Kh + k] = Cx<C>::mk((T)0.5 * (z.y + zc.y), (T)0.5 * (zc.x - z.x));
+    const int cc = min(Kh, scr / ldq);
+    for (int c0 = 0; c0 < Kh; c0 += cc) {
+        int ldr;
+        line_fft<C, false>(Q + c0 * ldq, ldq, Q + c0 * ldq, ldq, A, B, ldq, K1, min(cc, Kh - c0), F.rad[1],
+                           F.np[1], twy, &ldr);
+    }
+    C *out = static_cast<C *>(v.grid_cplx) + F.coff + (long long)x * K1 * Kh;
+    const float inv_kh = 1.0f / (float)Kh;
+    for (int e = threadIdx.x; e < K1 * Kh; e += blockDim.x) {
+        int y = quot(e, inv_kh), kz = e - y * Kh;
+        out[e] = Q[kz * ldq + y];
     }
 }
 
-// ---- y: columns of the half spectrum for fixed x, `cols` consecutive kz.
 template <typename C>
-__global__ void k_fft_y(DevView v, const FftSysDev *fs, const FftWork *work, int cols, int sign) {
+__global__ void __launch_bounds__(1024) k_fft_plane_inv(DevView v, const FftSysDev *fs, const FftWork *work,
+                                                        int twcap, int qcap, int scr) {
+    using T = typename Cx<C>::R;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    C *a = reinterpret_cast<C *>(smem_raw);
+    C *twy = reinterpret_cast<C *>(smem_raw);
     FftWork w = work[blockIdx.x];
     const FftSysDev &F = fs[w.sys];
-    int n = F.K[1], Kh = F.Kh;
-    int chunks = (Kh + cols - 1) / cols;
-    int x = w.unit / chunks, z0 = (w.unit - x * chunks) * cols;
-    int nc = min(cols, Kh - z0);
-    C *b = a + cols * n;
-    C *g = static_cast<C *>(v.grid_cplx) + F.coff + (long long)x * F.K[1] * Kh + z0;
-    // smem line c holds column z0 + c
-    for (int e = threadIdx.x; e < n * cols; e += blockDim.x) {
-        int y = e / cols, c = e - y * cols;
-        if (c < nc) a[c * n + y] = g[(long long)y * Kh + c];
-    }
+    const int K1 = F.K[1], K2 = F.K[2], Kh = F.Kh, x = w.unit;
+    const int ldq = K1 | 1, ldz = K2 | 1;
+    C *twz = twy + K1;
+    C *Q = twy + twcap;
+    C *A = Q + qcap;
+    C *B = A + scr;
+    load_tw(twy, v, F.tw[1], K1);
+    load_tw(twz, v, F.tw[2], K2);
+    const C *in = static_cast<const C *>(v.grid_cplx) + F.coff + (long long)x * K1 * Kh;
+    const float inv_kh = 1.0f / (float)Kh;
+    rounds<kRounds>(
+        K1 * Kh, [&](int e) { return in[e]; },
+        [&](int e, C val) {
+            int y = quot(e, inv_kh);
+            Q[(e - y * Kh) * ldq + y] = val;
+        });
     __syncthreads();
-    C *res = fft_lines(a, b, n, nc, F.rad[1], F.np[1], tw_table<C>(v, F.tw[1]), sign);
-    for (int e = threadIdx.x; e < n * cols; e += blockDim.x) {
-        int y = e / cols, c = e - y * cols;
-        if (c < nc) g[(long long)y * Kh + c] = res[c * n + y];
+    const int cc = min(Kh, scr / ldq);
+    for (int c0 = 0; c0 < Kh; c0 += cc) {
+        int ldr;
+        line_fft<C, true>(Q + c0 * ldq, ldq, Q + c0 * ldq, ldq, A, B, ldq, K1, min(cc, Kh - c0), F.rad[1], F.np[1],
+                          twy, &ldr);
+    }
+    T *out = static_cast<T *>(v.grid_real) + F.roff + (long long)x * K1 * K2;
+    const int npairs = (K1 + 1) >> 1, zc = min(npairs, scr / ldz);
+    for (int p0 = 0; p0 < npairs; p0 += zc) {
+        const int nc = min(zc, npairs - p0), y0 = 2 * p0;
+        z_inverse<C>(out + (long long)y0 * K2, K1 - y0, nc, K2, Kh, A, B, ldz, F, twz,
+                     [&](int p, int kk, int second) { return Q[kk * ldq + y0 + 2 * p + second]; });
     }
 }
 
-// ---- x: forward, convolution with the influence function, energy, inverse.
-template <typename C, typename ET>
-__global__ void k_fft_x_conv(DevView v, const FftSysDev *fs, const FftWork *work, int cols,
-                             int energy) {
-    using T = typename Cx<C>::R;
+// ================= line path: tiles of lines per block =================
+// Shared memory: the axis's twiddles (kmax words), two line buffers.
+
+// z forward: L real lines (L/2 complex) per block.
+template <typename C, typename Acc>
+__global__ void __launch_bounds__(256) k_fft_z_fwd(DevView v, const FftSysDev *fs, const FftWork *work, int L,
+                                                   int kmax) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    C *a = reinterpret_cast<C *>(smem_raw);
+    C *tw = reinterpret_cast<C *>(smem_raw);
     FftWork w = work[blockIdx.x];
     const FftSysDev &F = fs[w.sys];
-    int n = F.K[0], K1 = F.K[1], Kh = F.Kh;
-    int chunks = (Kh + cols - 1) / cols;
-    int y = w.unit / chunks, z0 = (w.unit - y * chunks) * cols;
-    int nc = min(cols, Kh - z0);
-    C *b = a + cols * n;
-    long long xstride = (long long)K1 * Kh;
-    C *g = static_cast<C *>(v.grid_cplx) + F.coff + (long long)y * Kh + z0;
-    for (int e = threadIdx.x; e < n * cols; e += blockDim.x) {
-        int x = e / cols, c = e - x * cols;
-        if (c < nc) a[c * n + x] = g[x * xstride + c];
-    }
+    const int n = F.K[2], Kh = F.Kh, ld = n | 1;
+    const int l0 = w.unit * L, nl = min(L, F.K[0] * F.K[1] - l0);
+    C *a = tw + kmax;
+    C *b = a + (L >> 1) * ld;
+    load_tw(tw, v, F.tw[2], n);
+    const Acc *acc = static_cast<const Acc *>(v.grid_acc) + F.roff + (long long)l0 * n;
+    C *out = static_cast<C *>(v.grid_cplx) + F.coff + (long long)l0 * Kh;
+    z_forward<C, Acc>(acc, nl, (nl + 1) >> 1, n, Kh, a, b, ld, F, tw, [&](int p, int k, C xa, C xb, bool hb) {
+        out[(long long)(2 * p) * Kh + k] = xa;
+        if (hb) out[(long long)(2 * p + 1) * Kh + k] = xb;
+    });
+}
+
+// y: columns of the half spectrum for fixed x, `cols` consecutive kz.
+template <typename C, bool INV>
+__global__ void __launch_bounds__(256) k_fft_y(DevView v, const FftSysDev *fs, const FftWork *work, int cols,
+                                               int kmax) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *tw = reinterpret_cast<C *>(smem_raw);
+    FftWork w = work[blockIdx.x];
+    const FftSysDev &F = fs[w.sys];
+    const int n = F.K[1], Kh = F.Kh, ld = n | 1;
+    const int chunks = (Kh + cols - 1) / cols;
+    const int x = w.unit / chunks, z0 = (w.unit - x * chunks) * cols;
+    const int nc = min(cols, Kh - z0);
+    C *a = tw + kmax;
+    C *b = a + cols * ld;
+    load_tw(tw, v, F.tw[1], n);
+    C *g = static_cast<C *>(v.grid_cplx) + F.coff + (long long)x * F.K[1] * Kh + z0;
+    const float inv_c = 1.0f / (float)nc;
+    // smem line c holds column z0 + c
+    rounds<kRounds>(
+        n * nc,
+        [&](int e) {
+            int y = quot(e, inv_c);
+            return g[(long long)y * Kh + e - y * nc];
+        },
+        [&](int e, C val) {
+            int y = quot(e, inv_c);
+            a[(e - y * nc) * ld + y] = val;
+        });
     __syncthreads();
-    C *res = fft_lines(a, b, n, nc, F.rad[0], F.np[0], tw_table<C>(v, F.tw[0]), -1);
+    int ldr;
+    C *res = line_fft<C, INV>(a, ld, nullptr, 0, b, a, ld, n, nc, F.rad[1], F.np[1], tw, &ldr);
+    for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
+        int y = quot(e, inv_c), c = e - y * nc;
+        g[(long long)y * Kh + c] = res[c * ldr + y];
+    }
+}
+
+// x: forward, convolution with the influence function, energy, inverse.
+// Used by both paths.
+template <typename C, typename ET>
+__global__ void __launch_bounds__(256) k_fft_x_conv(DevView v, const FftSysDev *fs, const FftWork *work, int cols,
+                                                    int kmax, int energy) {
+    using T = typename Cx<C>::R;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C *tw = reinterpret_cast<C *>(smem_raw);
+    FftWork w = work[blockIdx.x];
+    const FftSysDev &F = fs[w.sys];
+    const int n = F.K[0], K1 = F.K[1], Kh = F.Kh, ld = n | 1;
+    const int chunks = (Kh + cols - 1) / cols;
+    const int y = w.unit / chunks, z0 = (w.unit - y * chunks) * cols;
+    const int nc = min(cols, Kh - z0);
+    C *a = tw + kmax;
+    C *b = a + cols * ld;
+    load_tw(tw, v, F.tw[0], n);
+    const long long xstride = (long long)K1 * Kh;
+    C *g = static_cast<C *>(v.grid_cplx) + F.coff + (long long)y * Kh + z0;
+    const float inv_c = 1.0f / (float)nc, inv_n = 1.0f / (float)n;
+    rounds<kRounds>(
+        n * nc,
+        [&](int e) {
+            int x = quot(e, inv_c);
+            return g[x * xstride + e - x * nc];
+        },
+        [&](int e, C val) {
+            int x = quot(e, inv_c);
+            a[(e - x * nc) * ld + x] = val;
+        });
+    __syncthreads();
+    int ldr;
+    C *res = line_fft<C, false>(a, ld, nullptr, 0, b, a, ld, n, nc, F.rad[0], F.np[0], tw, &ldr);
     C *other = res == a ? b : a;
     const ET *et = static_cast<const ET *>(v.eterm) + F.coff + (long long)y * Kh + z0;
     double esum = 0.0;
-    for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
-        int c = e / n, kx = e - c * n;
-        int kz = z0 + c;
-        T f = (T)et[kx * xstride + c];
-        C s = res[c * n + kx];
-        if (energy) {
-            // half spectrum: planes kz = 0 and kz = K2/2 (even K2) appear once
-            double wgt = (kz == 0 || 2 * kz == F.K[2]) ? 1.0 : 2.0;
-            esum += wgt * (double)f * ((double)s.x * (double)s.x + (double)s.y * (double)s.y);
-        }
-        res[c * n + kx] = Cx<C>::mk(s.x * f, s.y * f);
-    }
+    rounds<kRounds>(
+        n * nc,
+        [&](int e) {
+            int c = quot(e, inv_n);
+            return (T)et[(e - c * n) * xstride + c];
+        },
+        [&](int e, T f) {
+            int c = quot(e, inv_n), kx = e - c * n;
+            int kz = z0 + c;
+            C s = res[c * ldr + kx];
+            if (energy) {
+                // half spectrum: planes kz = 0 and kz = K2/2 (even K2) appear once
+                double wgt = (kz == 0 || 2 * kz == F.K[2]) ? 1.0 : 2.0;
+                esum += wgt * (double)f * ((double)s.x * (double)s.x + (double)s.y * (double)s.y);
+            }
+            res[c * ldr + kx] = Cx<C>::mk(s.x * f, s.y * f);
+        });
     __syncthreads();
-    C *fin = fft_lines(res, other, n, nc, F.rad[0], F.np[0], tw_table<C>(v, F.tw[0]), +1);
-    for (int e = threadIdx.x; e < n * cols; e += blockDim.x) {
-        int x = e / cols, c = e - x * cols;
-        if (c < nc) g[x * xstride + c] = fin[c * n + x];
+    C *fin = line_fft<C, true>(res, ldr, nullptr, 0, other, res, ld, n, nc, F.rad[0], F.np[0], tw, &ldr);
+    for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
+        int x = quot(e, inv_c), c = e - x * nc;
+        g[x * xstride + c] = fin[c * ldr + x];
     }
     if (energy) energy_add(v.E, w.sys, E_RECIP, 0.5 * esum);
 }
 
-// ---- z inverse: half spectrum -> real grid.  Two Hermitian lines A, B are
-// completed and combined as Z = A + iB; the real and imaginary parts of the
-// inverse transform are the two real output lines.
+// z inverse: L real output lines per block.
 template <typename C>
-__global__ void k_fft_z_inv(DevView v, const FftSysDev *fs, const FftWork *work, int L) {
+__global__ void __launch_bounds__(256) k_fft_z_inv(DevView v, const FftSysDev *fs, const FftWork *work, int L,
+                                                   int kmax) {
     using T = typename Cx<C>::R;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    C *a = reinterpret_cast<C *>(smem_raw);
+    C *tw = reinterpret_cast<C *>(smem_raw);
     FftWork w = work[blockIdx.x];
     const FftSysDev &F = fs[w.sys];
-    int n = F.K[2], Kh = F.Kh;
-    int nl_total = F.K[0] * F.K[1];
-    int l0 = w.unit * L;
-    int nl = min(L, nl_total - l0);
-    int np2 = (nl + 1) >> 1;
-    C *b = a + (L >> 1) * n;
+    const int n = F.K[2], Kh = F.Kh, ld = n | 1;
+    const int l0 = w.unit * L, nl = min(L, F.K[0] * F.K[1] - l0);
+    C *a = tw + kmax;
+    C *b = a + (L >> 1) * ld;
+    load_tw(tw, v, F.tw[2], n);
     const C *in = static_cast<const C *>(v.grid_cplx) + F.coff + (long long)l0 * Kh;
-    for (int e = threadIdx.x; e < np2 * n; e += blockDim.x) {
-        int p = e / n, k = e - p * n;
-        bool upper = k >= Kh;
-        int kk = upper ? n - k : k;
-        C A = in[(long long)(2 * p) * Kh + kk];
-        C B = (2 * p + 1 < nl) ? in[(long long)(2 * p + 1) * Kh + kk] : Cx<C>::mk((T)0, (T)0);
-        if (upper) {
-            A.y = -A.y;
-            B.y = -B.y;
-        }
-        a[e] = Cx<C>::mk(A.x - B.y, A.y + B.x);
-    }
-    __syncthreads();
-    C *res = fft_lines(a, b, n, np2, F.rad[2], F.np[2], tw_table<C>(v, F.tw[2]), +1);
     T *out = static_cast<T *>(v.grid_real) + F.roff + (long long)l0 * n;
-    for (int e = threadIdx.x; e < np2 * n; e += blockDim.x) {
-        int p = e / n, z = e - p * n;
-        C r = res[e];
-        out[(long long)(2 * p) * n + z] = r.x;
-        if (2 * p + 1 < nl) out[(long long)(2 * p + 1) * n + z] = r.y;
-    }
+    z_inverse<C>(out, nl, (nl + 1) >> 1, n, Kh, a, b, ld, F, tw,
+                 [&](int p, int kk, int second) { return in[(long long)(2 * p + second) * Kh + kk]; });
 }
 
 template <typename C, typename Acc, typename ET>
 static void run(const DevView &v, const FftPlan &p, int energy, cudaStream_t st) {
     if (p.nz == 0) return;
-    k_fft_z_fwd<C, Acc><<<p.nz, 256, p.smem_z, st>>>(v, p.dsys, p.zwork, p.zlines);
-    k_fft_y<C><<<p.ny, 256, p.smem_y, st>>>(v, p.dsys, p.ywork, p.cols, -1);
-    k_fft_x_conv<C, ET><<<p.nx, 256, p.smem_x, st>>>(v, p.dsys, p.xwork, p.cols, energy);
-    k_fft_y<C><<<p.ny, 256, p.smem_y, st>>>(v, p.dsys, p.ywork, p.cols, +1);
-    k_fft_z_inv<C><<<p.nz, 256, p.smem_z, st>>>(v, p.dsys, p.zwork, p.zlines);
+    if (p.plane) {
+        k_fft_plane_fwd<C, Acc><<<p.npl, p.plane_threads, p.smem_plane, st>>>(v, p.dsys, p.pwork, p.twcap, p.qcap,
+                                                                            p.scr);
+        k_fft_x_conv<C, ET><<<p.nx, 256, p.smem_x, st>>>(v, p.dsys, p.xwork, p.cols, p.kmax, energy);
+        k_fft_plane_inv<C><<<p.npl, p.plane_threads, p.smem_plane, st>>>(v, p.dsys, p.pwork, p.twcap, p.qcap, p.scr);
+        return;
+    }
+    k_fft_z_fwd<C, Acc><<<p.nz, 256, p.smem_z, st>>>(v, p.dsys, p.zwork, p.zlines, p.kmax);
+    k_fft_y<C, false><<<p.ny, 256, p.smem_y, st>>>(v, p.dsys, p.ywork, p.cols, p.kmax);
+    k_fft_x_conv<C, ET><<<p.nx, 256, p.smem_x, st>>>(v, p.dsys, p.xwork, p.cols, p.kmax, energy);
+    k_fft_y<C, true><<<p.ny, 256, p.smem_y, st>>>(v, p.dsys, p.ywork, p.cols, p.kmax);
+    k_fft_z_inv<C><<<p.nz, 256, p.smem_z, st>>>(v, p.dsys, p.zwork, p.zlines, p.kmax);
 }
 
 void launch_fft_convolve(const DevView &v, const FftPlan &p, int energy, cudaStream_t st) {
@@ -318,6 +538,12 @@ void launch_fft_convolve(const DevView &v, const FftPlan &p, int energy, cudaStr
         run<float2, long long, float>(v, p, energy, st);
     else
         run<double2, double, double>(v, p, energy, st);
+}
+
+int fft_launch_count(const FftPlan &p) { return p.nz == 0 ? 0 : (p.plane ? 3 : 5); }
+
+size_t fft_line_smem(int lines, int kmax, size_t csz) {
+    return ((size_t)kmax + 2 * (size_t)lines * (size_t)(kmax | 1)) * csz;
 }
 
 static void factor(int n, int *rad, int *np) {
@@ -329,10 +555,41 @@ static void factor(int n, int *rad, int *np) {
     *np = k;
 }
 
+// Raises a kernel's dynamic shared-memory limit.  The limit is a per-kernel
+// attribute shared by every context (and plan) of the process on a device:
+// it is only ever raised, so a plan with smaller lines cannot lower it under
+// another one.  `slot` names the kernel (one per kernel and precision).
+static void raise_smem(const void *kernel, int slot, size_t bytes) {
+    static std::mutex mu;
+    static size_t seen[16][kMaxSmemDevices] = {};
+    if (bytes <= 48 * 1024) return;  // launches up to 48 KB need no attribute
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= kMaxSmemDevices) dev = 0;
+    std::lock_guard<std::mutex> lock(mu);
+    if (bytes <= seen[slot][dev]) return;
+    seen[slot][dev] = bytes;
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <typename C, typename Acc, typename ET>
+static void raise_all(const FftPlan &p, int base) {
+    raise_smem((const void *)k_fft_z_fwd<C, Acc>, base + 0, p.smem_z);
+    raise_smem((const void *)k_fft_z_inv<C>, base + 1, p.smem_z);
+    raise_smem((const void *)k_fft_y<C, false>, base + 2, p.smem_y);
+    raise_smem((const void *)k_fft_y<C, true>, base + 3, p.smem_y);
+    raise_smem((const void *)k_fft_x_conv<C, ET>, base + 4, p.smem_x);
+    if (p.plane_ok) {
+        raise_smem((const void *)k_fft_plane_fwd<C, Acc>, base + 5, p.smem_plane);
+        raise_smem((const void *)k_fft_plane_inv<C>, base + 6, p.smem_plane);
+    }
+}
+
 void fft_plan_build(FftPlan &p, int mixed) {
     // sizes and factorizations (lengths must be 2^a 3^b 5^c, checked by the caller)
-    std::vector<FftWork> z, y, x;
+    std::vector<FftWork> z, y, x, pl;
     p.kmax = 0;
+    int twcap = 0, qcap = 0, scr = 0, minscr = 0;
     for (int s = 0; s < p.S; ++s) {
         FftSysDev &F = p.hsys[s];
         for (int d = 0; d < 3; ++d) {
@@ -344,46 +601,46 @@ void fft_plan_build(FftPlan &p, int mixed) {
         int chunks = (F.Kh + p.cols - 1) / p.cols;
         for (int u = 0; u < F.K[0] * chunks; ++u) y.push_back({s, u});
         for (int u = 0; u < F.K[1] * chunks; ++u) x.push_back({s, u});
+        for (int u = 0; u < F.K[0]; ++u) pl.push_back({s, u});
+        // plane path geometry: whole-plane scratch when it fits
+        int ldq = F.K[1] | 1, ldz = F.K[2] | 1;
+        twcap = std::max(twcap, F.K[1] + F.K[2]);
+        qcap = std::max(qcap, F.Kh * ldq);
+        scr = std::max(scr, std::max(F.Kh * ldq, ((F.K[1] + 1) / 2) * ldz));
+        minscr = std::max(minscr, std::max(ldq, ldz));
     }
     size_t csz = mixed ? sizeof(float2) : sizeof(double2);
-    p.smem_z = 2 * (size_t)(p.zlines / 2) * p.kmax * csz;
-    p.smem_y = 2 * (size_t)p.cols * p.kmax * csz;
+    p.smem_z = fft_line_smem(p.zlines / 2, p.kmax, csz);
+    p.smem_y = fft_line_smem(p.cols, p.kmax, csz);
     p.smem_x = p.smem_y;
+    // the plane path keeps a plane and two scratch buffers in shared memory;
+    // the scratch shrinks to a chunk of lines when the plane is large
+    const size_t budget = 200 * 1024 / csz;
+    p.twcap = (twcap + 1) & ~1;  // keeps the next region 16-byte aligned
+    p.qcap = qcap;
+    long long room = (long long)budget - p.twcap - p.qcap;
+    p.scr = (int)std::min<long long>(scr, room / 2);
+    p.plane_ok = p.S > 0 && p.scr >= minscr;
+    if (!p.plane_ok) p.plane = 0;
+    p.smem_plane = ((size_t)p.twcap + p.qcap + 2 * (size_t)std::max(p.scr, 0)) * csz;
     cudaMalloc(&p.dsys, sizeof(FftSysDev) * p.S);
     cudaMemcpy(p.dsys, p.hsys.data(), sizeof(FftSysDev) * p.S, cudaMemcpyHostToDevice);
     p.nz = (int)z.size();
     p.ny = (int)y.size();
     p.nx = (int)x.size();
+    p.npl = (int)pl.size();
     cudaMalloc(&p.zwork, sizeof(FftWork) * (p.nz + 1));
     cudaMalloc(&p.ywork, sizeof(FftWork) * (p.ny + 1));
     cudaMalloc(&p.xwork, sizeof(FftWork) * (p.nx + 1));
+    cudaMalloc(&p.pwork, sizeof(FftWork) * (p.npl + 1));
     cudaMemcpy(p.zwork, z.data(), sizeof(FftWork) * p.nz, cudaMemcpyHostToDevice);
     cudaMemcpy(p.ywork, y.data(), sizeof(FftWork) * p.ny, cudaMemcpyHostToDevice);
     cudaMemcpy(p.xwork, x.data(), sizeof(FftWork) * p.nx, cudaMemcpyHostToDevice);
-    // The dynamic shared-memory limit is a per-kernel attribute shared by
-    // every context (and plan) of the process on a device: only ever raise
-    // it, so a plan with smaller lines cannot lower it under another one.
-    static std::mutex mu;
-    static int seen[2][kMaxSmemDevices] = {};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev < 0 || dev >= kMaxSmemDevices) dev = 0;
-    int big = (int)(p.smem_z > p.smem_y ? p.smem_z : p.smem_y);
-    std::lock_guard<std::mutex> lock(mu);
-    // launches up to 48 KB need no attribute
-    if (big <= 48 * 1024 || big <= seen[mixed ? 1 : 0][dev]) return;
-    seen[mixed ? 1 : 0][dev] = big;
-    if (mixed) {
-        cudaFuncSetAttribute(k_fft_z_fwd<float2, long long>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-        cudaFuncSetAttribute(k_fft_y<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-        cudaFuncSetAttribute(k_fft_x_conv<float2, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-        cudaFuncSetAttribute(k_fft_z_inv<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    } else {
-        cudaFuncSetAttribute(k_fft_z_fwd<double2, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-        cudaFuncSetAttribute(k_fft_y<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-        cudaFuncSetAttribute(k_fft_x_conv<double2, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-        cudaFuncSetAttribute(k_fft_z_inv<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    }
+    cudaMemcpy(p.pwork, pl.data(), sizeof(FftWork) * p.npl, cudaMemcpyHostToDevice);
+    if (mixed)
+        raise_all<float2, long long, float>(p, 0);
+    else
+        raise_all<double2, double, double>(p, 8);
 }
 
 void fft_plan_free(FftPlan &p) {
@@ -391,8 +648,9 @@ void fft_plan_free(FftPlan &p) {
     cudaFree(p.zwork);
     cudaFree(p.ywork);
     cudaFree(p.xwork);
+    cudaFree(p.pwork);
     p.dsys = nullptr;
-    p.zwork = p.ywork = p.xwork = nullptr;
+    p.zwork = p.ywork = p.xwork = p.pwork = nullptr;
 }
 
 }  // namespace nxm

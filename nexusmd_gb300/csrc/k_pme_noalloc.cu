@@ -381,8 +381,10 @@ extern "C" int nxm_pme_reciprocal_noalloc(const double *xyz, const double *charg
     plan.ny = g.K[0] * chunks;
     plan.nx = g.K[1] * chunks;
     plan.kmax = std::max(g.K[0], std::max(g.K[1], g.K[2]));
-    plan.smem_z = 2 * (size_t)(kZLines / 2) * plan.kmax * sizeof(float2);
-    plan.smem_y = 2 * (size_t)kCols * plan.kmax * sizeof(float2);
+    // line path (plan.plane = 0); at most 64 points per axis keeps every
+    // block under the 48 KB that needs no shared-memory attribute
+    plan.smem_z = fft_line_smem(kZLines / 2, plan.kmax, sizeof(float2));
+    plan.smem_y = fft_line_smem(kCols, plan.kmax, sizeof(float2));
     plan.smem_x = plan.smem_y;
     plan.dsys = reinterpret_cast<FftSysDev *>(scr + kOffSys);
     plan.zwork = reinterpret_cast<FftWork *>(scr + kOffWork);

@@ -40,6 +40,7 @@ void nxm_default_options(nxm_options *opt) {
     opt->autotune = 1;
     opt->report_threads = 4;
     opt->state_velocities = 0;
+    opt->fft_lines = 0;
 }
 
 static int code_for(const std::string &e) {
@@ -239,6 +240,12 @@ int nxm_get_tuning(nxm_ctx *ctx, int32_t out[3]) {
     if (!ctx || !out) return fail(NXM_ERR_INVALID, "null argument");
     const int *t = ctx->eng.tuning();
     for (int k = 0; k < 3; ++k) out[k] = t[k];
+    return NXM_OK;
+}
+
+int nxm_get_fft_plane_threads(nxm_ctx *ctx, int32_t *threads) {
+    if (!ctx || !threads) return fail(NXM_ERR_INVALID, "null argument");
+    *threads = ctx->eng.fft_plane_threads();
     return NXM_OK;
 }
 

@@ -647,6 +647,8 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         // FFT work lists only for systems with nonbonded forces: systems
         // without them keep an empty grid that no block touches
         fft_plan_build(plan_, mixed_);
+        plan_.plane = plan_.plane_ok && !opt.fft_lines;
+        tune_[0] = plan_.plane ? 0 : plan_.zlines;
     }
     v_.pme_block = 128;
     // systems without nonbonded forces: zero their charges in the PME and
@@ -685,8 +687,9 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
 // Launch shapes that change no result, chosen by timing each candidate on
 // this context's own buffers (grid contents do not matter for the timing;
 // what the timed kernels accumulate is cleared afterwards):
-//  * FFT: real lines per z-pass block x columns per y/x-pass block -- every
-//    line is transformed by the same arithmetic whatever the blocking;
+//  * FFT: threads per plane block (plane path) or real lines per z-pass
+//    block (line path), x columns per x-pass (and y-pass) block -- every line
+//    is transformed by the same arithmetic whatever the blocking;
 //  * spread / gather: threads per block -- the sums are integer atomics.
 // The neighbour-list cell groups are not tuned: their size changes the
 // summation order of the pair forces, and a choice that followed timing
@@ -705,25 +708,39 @@ std::string Engine::autotune() {
         cudaEventElapsedTime(&ms, a, b);
         return ms;
     };
+    // The path (plane or line) is fixed by the geometry and the options, not
+    // by timing: with odd K1 the two pair different z lines, and a choice
+    // that followed timing noise would break run-to-run bit reproducibility.
     float best = 1e30f;
-    int bz = plan_.zlines, bc = plan_.cols;
-    for (int zl : {8, 16, 32})
-        for (int cols : {4, 8, 16}) {
+    const int plane = plan_.plane;
+    int bz = plan_.zlines, bc = plan_.cols, bpt = plan_.plane_threads;
+    for (int cols : {4, 8, 16}) {
+        for (int zl : {8, 16, 32}) {
+            if (plane && zl != 16) continue;  // the z blocking is unused on the plane path
             fft_plan_free(plan_);
             plan_.zlines = zl;
             plan_.cols = cols;
             fft_plan_build(plan_, mixed_);
-            float t = time3([&] { launch_fft_convolve(v_, plan_, 0, st_); });
-            if (t < best) {
-                best = t;
-                bz = zl;
-                bc = cols;
+            plan_.plane = plane;
+            for (int th : {256, 512, 1024}) {
+                if (!plane && th != 256) continue;
+                plan_.plane_threads = th;
+                float t = time3([&] { launch_fft_convolve(v_, plan_, 0, st_); });
+                if (t < best) {
+                    best = t;
+                    bz = zl;
+                    bc = cols;
+                    bpt = th;
+                }
             }
         }
+    }
     fft_plan_free(plan_);
     plan_.zlines = bz;
     plan_.cols = bc;
     fft_plan_build(plan_, mixed_);
+    plan_.plane = plane;
+    plan_.plane_threads = bpt;
     best = 1e30f;
     int bt = v_.pme_block;
     for (int t : {64, 128, 256}) {
@@ -746,7 +763,7 @@ std::string Engine::autotune() {
     cudaStreamSynchronize(st_);
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    tune_[0] = bz;
+    tune_[0] = plan_.plane ? 0 : bz;
     tune_[1] = bc;
     tune_[2] = bt;
     return check("autotune");
@@ -792,10 +809,13 @@ std::string Engine::set_velocities(const double *xyz) {
 
 // Force kernels of one evaluation (everything but the integrator).
 // Kernel launches of force_launches below, without launching.
-static int force_launch_count(const DevView &v) {
+static int pme_launch_count(const DevView &v, const FftPlan &plan) {
+    return (v.N == 0 || plan.nz == 0) ? 0 : 2 + fft_launch_count(plan);
+}
+static int force_launch_count(const DevView &v, const FftPlan &plan) {
     bool nb = (v.force_mask & NXM_FORCE_NONBONDED) != 0;
     int n = (v.nb + v.na + v.nt + (nb ? v.nex + v.nxc : 0)) ? 1 : 0;
-    if (nb) n += 1 + 7;
+    if (nb) n += 1 + pme_launch_count(v, plan);
     return n;
 }
 
@@ -810,7 +830,7 @@ static int force_launches(const DevView &v, const FftPlan &plan, int energy, cud
     bool nb = (v.force_mask & NXM_FORCE_NONBONDED) != 0;
     if (nb && pme_st) {
         launch_pme(v, plan, energy, pme_st);
-        n += 7;
+        n += pme_launch_count(v, plan);
     }
     // bonded terms, exclusion correction and exceptions: one launch
     n += launch_bonded(v, energy, st, nb ? 1 : 0);
@@ -819,7 +839,7 @@ static int force_launches(const DevView &v, const FftPlan &plan, int energy, cud
         ++n;
         if (!pme_st) {
             launch_pme(v, plan, energy, st);
-            n += 7;
+            n += pme_launch_count(v, plan);
         }
     }
     return n;
@@ -911,7 +931,7 @@ std::string Engine::one_step(double dt, int report) {
         cudaError_t e = cudaGraphLaunch(G.exec, st_);
         if (e != cudaSuccess) return std::string("step graph launch: ") + cudaGetErrorString(e);
         // decide + forces + integrate; the rebuild kernels run on rebuild steps only
-        launches_per_step_ = force_launch_count(v_) + 2;
+        launches_per_step_ = force_launch_count(v_, plan_) + 2;
         return check("step");
     }
     if (report) cudaMemsetAsync(v_.E, 0, sizeof(long long) * v_.S * E_SLOTS, st_);

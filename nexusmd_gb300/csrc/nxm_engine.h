@@ -90,6 +90,8 @@ public:
     int launches_per_step() const { return launches_per_step_; }
     int launches_per_rebuild() const { return launches_per_rebuild_; }
     const int *tuning() const { return tune_; }
+    // threads per plane-path FFT block, 0 on the line path
+    int fft_plane_threads() const { return plan_.plane ? plan_.plane_threads : 0; }
     // neighbour-list rebuilds since creation, as of the last finished call
     long long rebuild_count() const { return h_flags_ ? reinterpret_cast<const Flags *>(h_flags_)->nrebuild : 0; }
 
@@ -105,9 +107,10 @@ private:
         bool ok = false;
     };
     StepGraph graph_[2];
-    // Launch shapes tuned at set-up: FFT real lines per z-pass block, FFT
-    // columns per y/x-pass block, threads per spread/gather block.
-    int tune_[3] = {16, 8, 128};
+    // Launch shapes tuned at set-up: FFT real lines per z-pass block (0 on
+    // the plane path), FFT columns per y/x-pass block, threads per
+    // spread/gather block.
+    int tune_[3] = {0, 8, 128};
     std::string autotune();
     std::string build_graph(double dt, int report);
     void free_graphs();

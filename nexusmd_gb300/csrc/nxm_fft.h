@@ -38,9 +38,23 @@ struct FftPlan {
     int cols = 8;       // z columns per block in the y and x passes
     size_t smem_z = 0, smem_y = 0, smem_x = 0;
     int kmax = 0;
+    // Plane path: one block per (system, x-plane) runs z then y forward and
+    // y then z inverse in shared memory (3 FFT launches instead of 5, the
+    // same arithmetic).  plane_ok when every system's plane fits.
+    FftWork *pwork = nullptr;
+    int npl = 0;
+    int plane = 0, plane_ok = 0;
+    int plane_threads = 512;
+    int twcap = 0, qcap = 0, scr = 0;   // shared-memory regions, complex words
+    size_t smem_plane = 0;
 };
 
 void fft_plan_build(FftPlan &plan, int mixed);
 void fft_plan_free(FftPlan &plan);
+// FFT kernel launches of one convolution with this plan.
+int fft_launch_count(const FftPlan &plan);
+// Shared memory of a line-path block: twiddles and two buffers of `lines`
+// lines of up to kmax complex words.
+size_t fft_line_smem(int lines, int kmax, size_t csz);
 
 }  // namespace nxm

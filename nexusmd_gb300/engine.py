@@ -42,7 +42,8 @@ class SystemDesc(C.Structure):
 class Options(C.Structure):
     _fields_ = [("precision", C.c_int32), ("skin", C.c_double), ("rebuild_interval", C.c_int32),
                 ("device", C.c_int32), ("max_neighbors", C.c_int32), ("exceptions", C.c_int32),
-                ("autotune", C.c_int32), ("report_threads", C.c_int32), ("state_velocities", C.c_int32)]
+                ("autotune", C.c_int32), ("report_threads", C.c_int32), ("state_velocities", C.c_int32),
+                ("fft_lines", C.c_int32)]
 
 
 class Energies(C.Structure):
@@ -91,6 +92,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.nxm_launches_per_step.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     L.nxm_rebuild_count.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
     L.nxm_get_tuning.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
+    L.nxm_get_fft_plane_threads.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
     L.nxm_n_atoms.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
     L.nxm_save_state.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_int64, C.c_double]
     _lib = L
@@ -116,12 +118,15 @@ class Engine:
 
     def __init__(self, systems, precision=PRECISION_MIXED, skin=0.1, rebuild_interval=10,
                  force_mask=FORCE_ALL, box="reference", grid=None, use_switch=0,
-                 switch_dist=0.0, exclusion_depth=3, max_neighbors=0, device=0, exceptions=False):
+                 switch_dist=0.0, exclusion_depth=3, max_neighbors=0, device=0, exceptions=False,
+                 fft_lines=False):
         """``box``: "reference" (extent + 1%, as the reference) or "explicit"
         (each system's periodic box [0, L)); ``grid``: None = each system's
         ``grid`` attribute, (0,0,0) = the reference's power-of-two rule;
         ``exceptions``: pass each system's ``exc_idx`` / ``exc_prm`` exception
-        pairs (OpenMM semantics) when it has them."""
+        pairs (OpenMM semantics) when it has them; ``fft_lines``: run the PME
+        FFT on the five-launch line path even where x-planes fit in shared
+        memory."""
         L = load_library()
         if not isinstance(systems, (list, tuple)):
             systems = [systems]
@@ -168,6 +173,7 @@ class Engine:
         L.nxm_default_options(C.byref(opt))
         opt.precision, opt.skin, opt.rebuild_interval = int(precision), float(skin), int(rebuild_interval)
         opt.device, opt.max_neighbors = int(device), int(max_neighbors)
+        opt.fft_lines = 1 if fft_lines else 0
         h = C.c_void_p()
         _check(L.nxm_create(descs, len(systems), C.byref(opt), np.concatenate(pos), C.byref(h)),
                "nxm_create")
@@ -271,10 +277,17 @@ class Engine:
         return a.value, b.value
 
     def tuning(self):
-        """Launch shapes in use: (FFT lines per z block, FFT columns per y/x block, spread/gather threads)."""
+        """Launch shapes in use: (FFT lines per z block or 0 on the plane path,
+        FFT columns per x block, spread/gather threads)."""
         out = (C.c_int32 * 3)()
         _check(self._L.nxm_get_tuning(self._h, out), "get_tuning")
         return tuple(out)
+
+    def fft_plane_threads(self):
+        """Threads per plane-path FFT block, 0 on the line path."""
+        t = C.c_int32()
+        _check(self._L.nxm_get_fft_plane_threads(self._h, C.byref(t)), "get_fft_plane_threads")
+        return t.value
 
     def rebuilds(self):
         """Neighbour-list rebuilds since the context was created."""
