@@ -104,12 +104,14 @@ typedef struct {
     int32_t state_velocities; /* Simulate only: 1 = start from the state XML's <Velocities>
                                  when it has one per atom; 0 (default) = zero velocities,
                                  as the reference */
-    int32_t fft_lines;        /* 0 (default): the PME FFT runs on the plane path (one block
-                                 per x-plane for the z and y transforms, 3 launches) when
-                                 every plane fits in shared memory; 1 = always the line
-                                 path (5 launches).  The same arithmetic: bit-equal results
-                                 when K1 is even; with odd K1 the z transforms pair other
-                                 lines, which changes only the rounding. */
+    int32_t fft_path;         /* PME FFT launch shape.  0 (default): the line path (5
+                                 launches over tiles of lines), or the plane path (one block
+                                 per x-plane for the z and y transforms, 3 launches) where
+                                 the autotuner finds it faster and every system's K1 is even
+                                 -- then both give the same numbers bit for bit; 1 = always
+                                 the line path; 2 = the plane path wherever the planes fit
+                                 in shared memory (with odd K1 the z transforms pair other
+                                 lines than on the line path, which changes the rounding). */
 } nxm_options;
 
 /* Energies of one system (kJ/mol) at the last evaluation that computed them. */

@@ -28,7 +28,7 @@ class _Opts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("skin", C.c_double), ("rebuild_interval", C.c_int32),
                 ("device", C.c_int32), ("max_neighbors", C.c_int32), ("exceptions", C.c_int32),
                 ("autotune", C.c_int32), ("report_threads", C.c_int32), ("state_velocities", C.c_int32),
-                ("fft_lines", C.c_int32)]
+                ("fft_path", C.c_int32)]
 
 
 def _lib():

@@ -40,7 +40,7 @@ void nxm_default_options(nxm_options *opt) {
     opt->autotune = 1;
     opt->report_threads = 4;
     opt->state_velocities = 0;
-    opt->fft_lines = 0;
+    opt->fft_path = 0;
 }
 
 static int code_for(const std::string &e) {

@@ -183,6 +183,8 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return "no CUDA device";
     if (opt.device < 0 || opt.device >= ndev) return "bad device ordinal";
+    if (opt.fft_path < 0 || opt.fft_path > 2) return "bad fft_path";
+    fft_path_ = opt.fft_path;
     cudaSetDevice(opt.device);
     device_ = opt.device;
     mixed_ = opt.precision == NXM_PRECISION_MIXED ? 1 : 0;
@@ -647,7 +649,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         // FFT work lists only for systems with nonbonded forces: systems
         // without them keep an empty grid that no block touches
         fft_plan_build(plan_, mixed_);
-        plan_.plane = plan_.plane_ok && !opt.fft_lines;
+        plan_.plane = plan_.plane_ok && fft_path_ == 2;
         tune_[0] = plan_.plane ? 0 : plan_.zlines;
     }
     v_.pme_block = 128;
@@ -708,29 +710,37 @@ std::string Engine::autotune() {
         cudaEventElapsedTime(&ms, a, b);
         return ms;
     };
-    // The path (plane or line) is fixed by the geometry and the options, not
-    // by timing: with odd K1 the two pair different z lines, and a choice
-    // that followed timing noise would break run-to-run bit reproducibility.
+    // The plane path joins the line path as a candidate only where the two
+    // give the same numbers bit for bit (every system's K1 even: the z
+    // transforms pair the same real lines), so that a pick that follows
+    // timing noise cannot change results; fft_path 1 / 2 fix the path.
+    bool even_k1 = true;
+    for (int s = 0; s < plan_.S; ++s) even_k1 = even_k1 && plan_.hsys[s].K[1] % 2 == 0;
+    const bool try_line = fft_path_ != 2 || !plan_.plane_ok;
+    const bool try_plane = plan_.plane_ok && (fft_path_ == 2 || (fft_path_ == 0 && even_k1));
     float best = 1e30f;
-    const int plane = plan_.plane;
-    int bz = plan_.zlines, bc = plan_.cols, bpt = plan_.plane_threads;
+    int bz = plan_.zlines, bc = plan_.cols, bp = plan_.plane, bpt = plan_.plane_threads;
     for (int cols : {4, 8, 16}) {
         for (int zl : {8, 16, 32}) {
-            if (plane && zl != 16) continue;  // the z blocking is unused on the plane path
+            if (!try_line && zl != 16) continue;  // the z blocking is unused on the plane path
             fft_plan_free(plan_);
             plan_.zlines = zl;
             plan_.cols = cols;
             fft_plan_build(plan_, mixed_);
-            plan_.plane = plane;
-            for (int th : {256, 512, 1024}) {
-                if (!plane && th != 256) continue;
-                plan_.plane_threads = th;
-                float t = time3([&] { launch_fft_convolve(v_, plan_, 0, st_); });
-                if (t < best) {
-                    best = t;
-                    bz = zl;
-                    bc = cols;
-                    bpt = th;
+            for (int plane = 0; plane < 2; ++plane) {
+                if (plane ? !(try_plane && zl == 16) : !try_line) continue;
+                plan_.plane = plane;
+                for (int th : {256, 512, 1024}) {
+                    if (!plane && th != 256) continue;
+                    plan_.plane_threads = th;
+                    float t = time3([&] { launch_fft_convolve(v_, plan_, 0, st_); });
+                    if (t < best) {
+                        best = t;
+                        bz = zl;
+                        bc = cols;
+                        bp = plane;
+                        bpt = th;
+                    }
                 }
             }
         }
@@ -739,7 +749,7 @@ std::string Engine::autotune() {
     plan_.zlines = bz;
     plan_.cols = bc;
     fft_plan_build(plan_, mixed_);
-    plan_.plane = plane;
+    plan_.plane = bp;
     plan_.plane_threads = bpt;
     best = 1e30f;
     int bt = v_.pme_block;

@@ -131,6 +131,7 @@ private:
     int device_ = 0;
     int mixed_ = 1;
     int interval_ = 1;
+    int fft_path_ = 0;  // nxm_options::fft_path
     bool force_rebuild_ = true;
     int since_rebuild_ = 0;
     std::vector<void *> allocs_;

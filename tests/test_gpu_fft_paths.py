@@ -21,9 +21,9 @@ pytestmark = pytest.mark.gpu
 TERMS = ("recip", "self", "coulomb", "vdw", "exclusion")
 
 
-def _run(s, grid, precision, fft_lines):
+def _run(s, grid, precision, fft_path):
     from nexusmd_gb300.engine import Engine
-    eng = Engine(s, precision=precision, skin=0.0, rebuild_interval=1, grid=grid, fft_lines=fft_lines)
+    eng = Engine(s, precision=precision, skin=0.0, rebuild_interval=1, grid=grid, fft_path=fft_path)
     try:
         tune = eng.tuning() + (eng.fft_plane_threads(),)
         return eng.compute_forces(), eng.energies(), tune
@@ -43,8 +43,8 @@ def test_plane_and_line_paths_agree_with_oracle(oracle, c1_compat, grid):
     F0, E0 = oracle.forces(oracle.describe(s, grid=grid), s.pos, box, eoff, el)
     scale = max(abs(E0[k]) for k in TERMS)
     for precision, ftol, etol in ((1, 1e-5, 2e-5), (0, 1e-9, 1e-9)):
-        Fp, Ep, tp = _run(s, grid, precision, False)
-        Fl, El, tl = _run(s, grid, precision, True)
+        Fp, Ep, tp = _run(s, grid, precision, 2)
+        Fl, El, tl = _run(s, grid, precision, 1)
         assert tl[0] > 0 and tl[3] == 0  # the line path reports its z blocking
         if precision == 1:
             # every mixed case here fits the plane path
@@ -58,3 +58,18 @@ def test_plane_and_line_paths_agree_with_oracle(oracle, c1_compat, grid):
             assert Ep["recip"] == El["recip"]
         else:
             assert _rel_rms(Fp, Fl) <= (1e-6 if precision == 1 else 1e-12), (grid, _rel_rms(Fp, Fl))
+
+
+def test_autotuned_path_gives_the_line_path_numbers(c1_compat):
+    """fft_path 0 lets the autotuner pick either path only where both give
+    the same bits (K1 even), so the pick cannot change results."""
+    grid = (24, 30, 20)
+    Fa, Ea, _ = _run(c1_compat, grid, 1, 0)
+    Fl, El, _ = _run(c1_compat, grid, 1, 1)
+    assert np.array_equal(Fa, Fl) and Ea["recip"] == El["recip"]
+
+
+def test_bad_fft_path_is_rejected(c1_compat):
+    from nexusmd_gb300.engine import Engine, NxmError
+    with pytest.raises(NxmError, match="fft_path"):
+        Engine(c1_compat, precision=1, grid=(24, 30, 20), fft_path=3)
