@@ -356,6 +356,62 @@ __device__ __forceinline__ void pair_mixed(bool in, float dx, float dy, float dz
     }
 }
 
+// Per-system constants of pair_mixed2, each in both halves of a float2.
+struct PairPrm2 {
+    float2 ex2c, a04, k2a, one, twelve, msix, mone;
+};
+
+__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
+
+__device__ __forceinline__ float2 erfcx_fit2(float2 t) {
+    float2 g = dup2(-2.164941738e-01f);
+    g = __ffma2_rn(g, t, dup2(7.803782561e-01f));
+    g = __ffma2_rn(g, t, dup2(-4.985805536e-01f));
+    g = __ffma2_rn(g, t, dup2(5.875147125e-01f));
+    g = __ffma2_rn(g, t, dup2(1.009222009e-01f));
+    g = __ffma2_rn(g, t, dup2(2.479314205e-01f));
+    g = __ffma2_rn(g, t, dup2(-1.671998421e-03f));
+    return g;
+}
+
+// pair_mixed for a lane's two entries at once (no switching function): the
+// same chain of operations per entry in the two halves of packed FP32x2
+// arithmetic, one instruction for both entries (the reciprocal square root,
+// exponential and reciprocal stay scalar); about a sixth fewer instructions
+// per entry.  The displacements come as j - i, so the force sums (fxy = x,
+// y; fz) are negated sums; the caller flips their sign.
+template <bool ENERGY>
+__device__ __forceinline__ void pair_mixed2(bool in0, bool in1, float2 dxy0, float dz0, float2 dxy1, float dz1,
+                                            float2 r2, float2 qq, float2 sg, float2 eps, const PairPrm2 &P,
+                                            float2 &fxy, float &fz, float &ec, float &ev) {
+    float2 rinv = make_float2(fast_rsqrt(r2.x), fast_rsqrt(r2.y));
+    float2 rinv2 = __fmul2_rn(rinv, rinv);
+    float2 r = __fmul2_rn(r2, rinv);
+    float2 ea = __fmul2_rn(r2, P.ex2c);
+    float2 ex = make_float2(fast_ex2(ea.x), fast_ex2(ea.y));
+    float2 tt = __ffma2_rn(P.a04, r, P.one);
+    float2 erfcv = __fmul2_rn(ex, erfcx_fit2(make_float2(fast_rcp(tt.x), fast_rcp(tt.y))));
+    float2 qr = __fmul2_rn(qq, rinv);
+    float2 dEdR = __fmul2_rn(__fmul2_rn(qr, rinv2), __ffma2_rn(__fmul2_rn(P.k2a, r), ex, erfcv));
+    float2 s2 = __fmul2_rn(__fmul2_rn(sg, sg), rinv2);
+    float2 s6 = __fmul2_rn(__fmul2_rn(s2, s2), s2);
+    float2 lj = __fmul2_rn(__fmul2_rn(eps, __ffma2_rn(P.twelve, s6, P.msix)), s6);
+    dEdR = __ffma2_rn(lj, rinv2, dEdR);
+    const float d0 = in0 ? dEdR.x : 0.0f, d1 = in1 ? dEdR.y : 0.0f;
+    fxy = __ffma2_rn(dxy0, dup2(d0), fxy);
+    fz = fmaf(dz0, d0, fz);
+    fxy = __ffma2_rn(dxy1, dup2(d1), fxy);
+    fz = fmaf(dz1, d1, fz);
+    if (ENERGY) {
+        float2 e = __fmul2_rn(qr, erfcv);
+        float2 evdw = __fmul2_rn(__fmul2_rn(eps, __fadd2_rn(s6, P.mone)), s6);
+        ec += in0 ? e.x : 0.0f;
+        ev += in0 ? evdw.x : 0.0f;
+        ec += in1 ? e.y : 0.0f;
+        ev += in1 ? evdw.y : 0.0f;
+    }
+}
+
 // Mixed precision: each lane keeps two list entries in flight; j comes from
 // the staged tile.  SW: some system of the batch uses the switching function.
 template <bool ENERGY, bool SW>
@@ -394,6 +450,7 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_pairs_mixed(DevView v) {
     int czf = (c3f >> 20) & 1023;
     const float lo = S.cut2f_lo, hi = S.cut2f_hi;
     const PairPrm P{S.ex2c, S.a04, S.k2a, S.sw_distf, S.cutofff, S.use_switch};
+    const PairPrm2 P2{dup2(S.ex2c), dup2(S.a04), dup2(S.k2a), dup2(1.0f), dup2(12.0f), dup2(-6.0f), dup2(-1.0f)};
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     float ec = 0.f, ev = 0.f;
     for (int i = a0 + warp; i < a1; i += nw) {
@@ -404,6 +461,10 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_pairs_mixed(DevView v) {
         const int cnt = v.ncount[i];
         const uint4 *lst4 = reinterpret_cast<const uint4 *>(v.nl16 + (size_t)i * v.stride) + lane;
         float fx = 0.f, fy = 0.f, fz = 0.f;
+        // without the switching function: negated x, y sums as a pair (pair_mixed2)
+        float2 fxy = make_float2(0.f, 0.f);
+        const float2 nxy = make_float2(-pi3[0], -pi3[1]);
+        const float nz = -pi3[2];
         // the first chunk's slot always exists: its load need not wait for the count
         uint4 cur = __ldg(lst4);
         for (int c0 = 0; c0 < cnt; c0 += 256) {
@@ -423,10 +484,12 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_pairs_mixed(DevView v) {
                     int t1 = v1 ? (int)(wds[u >> 1] >> 16) : 0;
                     float4 p0 = s_q[t0], p1 = s_q[t1];
                     float2 l0 = s_lj[t0], l1 = s_lj[t1];
-                    float dx0 = pi3[0] - p0.x, dy0 = pi3[1] - p0.y, dz0 = pi3[2] - p0.z;
-                    float dx1 = pi3[0] - p1.x, dy1 = pi3[1] - p1.y, dz1 = pi3[2] - p1.z;
-                    float r20 = v0 ? dx0 * dx0 + dy0 * dy0 + dz0 * dz0 : 1e30f;
-                    float r21 = v1 ? dx1 * dx1 + dy1 * dy1 + dz1 * dz1 : 1e30f;
+                    // j - i: x and y as one pair per entry
+                    const float2 dxy0 = __fadd2_rn(make_float2(p0.x, p0.y), nxy);
+                    const float2 dxy1 = __fadd2_rn(make_float2(p1.x, p1.y), nxy);
+                    const float dz0 = p0.z + nz, dz1 = p1.z + nz;
+                    float r20 = v0 ? fmaf(dz0, dz0, fmaf(dxy0.y, dxy0.y, dxy0.x * dxy0.x)) : 1e30f;
+                    float r21 = v1 ? fmaf(dz1, dz1, fmaf(dxy1.y, dxy1.y, dxy1.x * dxy1.x)) : 1e30f;
                     bool in0 = r20 < lo, in1 = r21 < lo;
                     bool b0 = !in0 && r20 < hi, b1 = !in1 && r21 < hi;
                     if (__any_sync(full, b0 || b1)) {
@@ -434,10 +497,16 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_pairs_mixed(DevView v) {
                         if (b0) in0 = exact_r2(v, S, i, hood_slot(spans, nsp, t0)) < S.cut2;
                         if (b1) in1 = exact_r2(v, S, i, hood_slot(spans, nsp, t1)) < S.cut2;
                     }
-                    pair_mixed<ENERGY, SW>(in0, dx0, dy0, dz0, r20, qi * p0.w, li.x + l0.x, li.y * l0.y, P, fx, fy,
-                                           fz, ec, ev);
-                    pair_mixed<ENERGY, SW>(in1, dx1, dy1, dz1, r21, qi * p1.w, li.x + l1.x, li.y * l1.y, P, fx, fy,
-                                           fz, ec, ev);
+                    if (SW) {
+                        pair_mixed<ENERGY, SW>(in0, -dxy0.x, -dxy0.y, -dz0, r20, qi * p0.w, li.x + l0.x,
+                                               li.y * l0.y, P, fx, fy, fz, ec, ev);
+                        pair_mixed<ENERGY, SW>(in1, -dxy1.x, -dxy1.y, -dz1, r21, qi * p1.w, li.x + l1.x,
+                                               li.y * l1.y, P, fx, fy, fz, ec, ev);
+                    } else {
+                        pair_mixed2<ENERGY>(in0, in1, dxy0, dz0, dxy1, dz1, make_float2(r20, r21),
+                                            make_float2(qi * p0.w, qi * p1.w), make_float2(li.x + l0.x, li.x + l1.x),
+                                            make_float2(li.y * l0.y, li.y * l1.y), P2, fxy, fz, ec, ev);
+                    }
                 }
             };
             if (c0 + 256 <= cnt)
@@ -445,6 +514,11 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_pairs_mixed(DevView v) {
             else
                 walk(std::false_type{});
             cur = nxt;
+        }
+        if (!SW) {
+            fx = -fxy.x;
+            fy = -fxy.y;
+            fz = -fz;
         }
         fx = warp_sum(fx);
         fy = warp_sum(fy);
