@@ -469,7 +469,9 @@ __global__ void __launch_bounds__(256) k_fft_x_conv(DevView v, const FftSysDev *
     C *res = line_fft<C, false>(a, ld, nullptr, 0, b, a, ld, n, nc, F.rad[0], F.np[0], tw, &ldr);
     C *other = res == a ? b : a;
     const ET *et = static_cast<const ET *>(v.eterm) + F.coff + (long long)y * Kh + z0;
-    double esum = 0.0;
+    // the energy in fixed point per element: its sum is the same whatever
+    // the column blocking (an autotuned launch shape) groups together
+    long long esum = 0;
     rounds<kRounds>(
         n * nc,
         [&](int e) {
@@ -481,9 +483,10 @@ __global__ void __launch_bounds__(256) k_fft_x_conv(DevView v, const FftSysDev *
             int kz = z0 + c;
             C s = res[c * ldr + kx];
             if (energy) {
-                // half spectrum: planes kz = 0 and kz = K2/2 (even K2) appear once
-                double wgt = (kz == 0 || 2 * kz == F.K[2]) ? 1.0 : 2.0;
-                esum += wgt * (double)f * ((double)s.x * (double)s.x + (double)s.y * (double)s.y);
+                // half spectrum: planes kz = 0 and kz = K2/2 (even K2) appear
+                // once; E = sum / 2
+                double wgt = (kz == 0 || 2 * kz == F.K[2]) ? 0.5 * kEnergyScale : kEnergyScale;
+                esum += __double2ll_rn(wgt * (double)f * ((double)s.x * (double)s.x + (double)s.y * (double)s.y));
             }
             res[c * ldr + kx] = Cx<C>::mk(s.x * f, s.y * f);
         });
@@ -493,7 +496,7 @@ __global__ void __launch_bounds__(256) k_fft_x_conv(DevView v, const FftSysDev *
         int x = quot(e, inv_c), c = e - x * nc;
         g[x * xstride + c] = fin[c * ldr + x];
     }
-    if (energy) energy_add(v.E, w.sys, E_RECIP, 0.5 * esum);
+    if (energy) energy_add_fixed(v.E, w.sys, E_RECIP, esum);
 }
 
 // z inverse: L real output lines per block.

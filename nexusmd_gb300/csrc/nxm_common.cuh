@@ -166,6 +166,15 @@ __device__ __forceinline__ void energy_add(long long *E, int sys, int term, doub
     }
 }
 
+// Adds one fixed-point energy per lane (units of 1 / kEnergyScale) of a
+// warp whose lanes all belong to system `sys`: integer sums, so the total does
+// not depend on how the contributions were grouped into lanes and warps.
+__device__ __forceinline__ void energy_add_fixed(long long *E, int sys, int term, long long v) {
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v != 0)
+        atomicAdd(reinterpret_cast<unsigned long long *>(&E[sys * E_SLOTS + term]), static_cast<unsigned long long>(v));
+}
+
 // erfc(x) = exp(-x^2) * g(t), t = 1 / (1 + 0.4 x), x in [0, 4]: degree-6
 // least-squares fit of the scaled complementary error function on Chebyshev
 // nodes of t, max relative error 5e-7 in FP32 (derivation and error table:
