@@ -130,6 +130,12 @@ typedef struct {
 typedef struct nxm_ctx nxm_ctx;
 
 const char *nxm_version(void);
+
+/* FP32 fused multiply-add throughput of a device (TFLOP/s, 2 flops per FMA):
+ * scalar FFMA and packed FP32x2 FFMA2, each the best of 5 timed launches of a
+ * probe kernel that keeps every SM busy.  The roofline denominator of the
+ * FP32-bound pair kernel.  Runs its own stream; no context needed. */
+int nxm_fp32_peak(int32_t device, double *tflops_scalar, double *tflops_packed);
 const char *nxm_last_error(void);
 void nxm_default_options(nxm_options *opt);
 
