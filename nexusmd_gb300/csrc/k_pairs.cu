@@ -140,6 +140,15 @@ __device__ __forceinline__ int list_pos(int p) { return (p & ~255) | ((p & 31) <
 // within the z extent the sphere has over that row, found by binary search
 // (0.01 nm margin), in tile order: the list is the one a scan of the whole
 // tile gives.
+// Stores one 256-entry list chunk held in order in shared memory as the list
+// layout wants it: lane l writes 16 bytes, entries l + 32 q for q = 0..7.
+__device__ __forceinline__ void store_chunk(uint16_t *dst, const uint16_t *src, int lane) {
+    uint32_t w[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) w[q] = (uint32_t)src[lane + 64 * q] | ((uint32_t)src[lane + 64 * q + 32] << 16);
+    reinterpret_cast<uint4 *>(dst)[lane] = make_uint4(w[0], w[1], w[2], w[3]);
+}
+
 __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_build(DevView v) {
     extern __shared__ __align__(16) unsigned char smem[];
     if (!v.flags->rebuild) return;
@@ -247,9 +256,10 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_build(DevView v) {
                 }
             }
         }
-        // i's list is assembled per 256-entry chunk, transposed as in memory,
-        // in two halves per warp: entry p goes to half (p >> 8) & 1, so an
-        // iteration that completes a chunk writes on into the other half
+        // i's list is assembled per 256-entry chunk in two halves per warp
+        // (entry p at p & 511), so an iteration that completes a chunk writes
+        // on into the other half; a completed chunk is stored transposed as
+        // in memory (lane l's 16 bytes hold entries l + 32 q, q = 0..7)
         uint16_t *buf = s_buf + warp * 512;
         const unsigned lt = (1u << lane) - 1u;
         unsigned rows = __ballot_sync(full, ke > kb);
@@ -272,16 +282,17 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_build(DevView v) {
                         for (int e = 32; e < ne; ++e) ex |= (v.excl_lst[e0 + e] == oj);
                     m = __ballot_sync(full, cand && !ex);
                 }
-                const int pos = count + __popc(m & lt);
-                if ((m >> lane) & 1u) buf[((pos >> 8) & 1) * 256 + ((pos & 31) << 3) + ((pos >> 5) & 7)] = (uint16_t)k;
                 const int newc = count + __popc(m);
+                // every lane stores: a rejected candidate goes to newc + lane,
+                // past the entries so far -- a slot that a later entry
+                // overwrites or that lies beyond the list's count (never in
+                // the half being stored: at most 32 entries come per iteration)
+                buf[(((m >> lane) & 1u) ? count + __popc(m & lt) : newc + lane) & 511] = (uint16_t)k;
                 if ((newc ^ count) >> 8) {
                     // chunk count >> 8 complete: one 16-byte store per lane
                     __syncwarp();
                     const int c = count >> 8;
-                    if ((c + 1) * 256 <= v.stride)
-                        reinterpret_cast<uint4 *>(out + c * 256)[lane] =
-                            reinterpret_cast<const uint4 *>(buf + (c & 1) * 256)[lane];
+                    if ((c + 1) * 256 <= v.stride) store_chunk(out + c * 256, buf + (c & 1) * 256, lane);
                     __syncwarp();
                 }
                 count = newc;
@@ -290,8 +301,7 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_build(DevView v) {
         __syncwarp();
         {
             const int c = count >> 8;
-            if ((count & 255) && c * 256 < v.stride)
-                reinterpret_cast<uint4 *>(out + c * 256)[lane] = reinterpret_cast<const uint4 *>(buf + (c & 1) * 256)[lane];
+            if ((count & 255) && c * 256 < v.stride) store_chunk(out + c * 256, buf + (c & 1) * 256, lane);
         }
         __syncwarp();
         if (lane == 0) {
