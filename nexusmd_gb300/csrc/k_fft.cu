@@ -105,11 +105,11 @@ __device__ __forceinline__ int quot(int a, float inv_d) { return (int)(((float)a
 // holds W_n^t = exp(-2 pi i t / n); conjugated for the inverse), and writes
 // (j div Ns) Ns R + (j mod Ns) + r Ns.
 template <typename C, int R, bool INV>
-__device__ __forceinline__ void stockham(const C *src, int lds, C *dst, int ldd, int n, int nl, int Ns,
+__device__ __forceinline__ void stockham(const C *src, int lds, C *dst, int ldd, int nl, const FftPasses &P, int p,
                                          const C *tw) {
     using T = typename Cx<C>::R;
-    const int m = n / R, step = n / (Ns * R), tot = nl * m;
-    const float inv_m = 1.0f / (float)m, inv_ns = 1.0f / (float)Ns;
+    const int m = P.m[p], Ns = P.Ns[p], step = P.step[p], tot = nl * m;
+    const float inv_m = P.inv_m[p], inv_ns = P.inv_ns[p];
     for (int bi = threadIdx.x; bi < tot; bi += blockDim.x) {
         int l = quot(bi, inv_m), j = bi - l * m;
         int jq = quot(j, inv_ns), k = j - jq * Ns;
@@ -140,10 +140,11 @@ __device__ __forceinline__ void stockham(const C *src, int lds, C *dst, int ldd,
 // copied).  Returns the buffer holding the result and sets *ldr to its line
 // stride.  Ends with a barrier.
 template <typename C, bool INV>
-__device__ C *line_fft(C *in, int ldi, C *out, int ldo, C *s0, C *s1, int lds, int n, int nl, const int *rad,
-                       int np, const C *tw, int *ldr) {
+__device__ C *line_fft(C *in, int ldi, C *out, int ldo, C *s0, C *s1, int lds, int n, int nl, const FftPasses &P,
+                       const C *tw, int *ldr) {
     C *src = in;
-    int ls = ldi, Ns = 1;
+    int ls = ldi;
+    const int np = P.np;
     for (int p = 0; p < np; ++p) {
         C *dst = (p & 1) ? s1 : s0;
         int ld = lds;
@@ -151,16 +152,15 @@ __device__ C *line_fft(C *in, int ldi, C *out, int ldo, C *s0, C *s1, int lds, i
             dst = out;
             ld = ldo;
         }
-        switch (rad[p]) {
-            case 4: stockham<C, 4, INV>(src, ls, dst, ld, n, nl, Ns, tw); break;
-            case 2: stockham<C, 2, INV>(src, ls, dst, ld, n, nl, Ns, tw); break;
-            case 3: stockham<C, 3, INV>(src, ls, dst, ld, n, nl, Ns, tw); break;
-            default: stockham<C, 5, INV>(src, ls, dst, ld, n, nl, Ns, tw); break;
+        switch (P.R[p]) {
+            case 4: stockham<C, 4, INV>(src, ls, dst, ld, nl, P, p, tw); break;
+            case 2: stockham<C, 2, INV>(src, ls, dst, ld, nl, P, p, tw); break;
+            case 3: stockham<C, 3, INV>(src, ls, dst, ld, nl, P, p, tw); break;
+            default: stockham<C, 5, INV>(src, ls, dst, ld, nl, P, p, tw); break;
         }
         __syncthreads();
         src = dst;
         ls = ld;
-        Ns *= rad[p];
     }
     if (out && src != out) {
         const float inv_n = 1.0f / (float)n;
@@ -239,7 +239,7 @@ __device__ __forceinline__ void z_forward(const Acc *acc, int nreal, int nc, int
         });
     __syncthreads();
     int ldr;
-    C *res = line_fft<C, false>(a, ld, nullptr, 0, b, a, ld, n, nc, F.rad[2], F.np[2], tw, &ldr);
+    C *res = line_fft<C, false>(a, ld, nullptr, 0, b, a, ld, n, nc, F.ax[2], tw, &ldr);
     for (int e = threadIdx.x; e < nc * Kh; e += blockDim.x) {
         int p = quot(e, inv_kh), k = e - p * Kh;
         C z = res[p * ldr + k];
@@ -280,7 +280,7 @@ __device__ __forceinline__ void z_inverse(typename Cx<C>::R *out, int nreal, int
         });
     __syncthreads();
     int ldr;
-    C *res = line_fft<C, true>(a, ld, nullptr, 0, b, a, ld, n, nc, F.rad[2], F.np[2], tw, &ldr);
+    C *res = line_fft<C, true>(a, ld, nullptr, 0, b, a, ld, n, nc, F.ax[2], tw, &ldr);
     for (int e = threadIdx.x; e < nc * n; e += blockDim.x) {
         int p = quot(e, inv_n), z = e - p * n;
         C r = res[p * ldr + z];
@@ -322,8 +322,8 @@ __global__ void __launch_bounds__(1024) k_fft_plane_fwd(DevView v, const FftSysD
     const int cc = min(Kh, scr / ldq);
     for (int c0 = 0; c0 < Kh; c0 += cc) {
         int ldr;
-        line_fft<C, false>(Q + c0 * ldq, ldq, Q + c0 * ldq, ldq, A, B, ldq, K1, min(cc, Kh - c0), F.rad[1],
-                           F.np[1], twy, &ldr);
+        line_fft<C, false>(Q + c0 * ldq, ldq, Q + c0 * ldq, ldq, A, B, ldq, K1, min(cc, Kh - c0), F.ax[1], twy,
+                           &ldr);
     }
     C *out = static_cast<C *>(v.grid_cplx) + F.coff + (long long)x * K1 * Kh;
     const float inv_kh = 1.0f / (float)Kh;
@@ -361,8 +361,8 @@ __global__ void __launch_bounds__(1024) k_fft_plane_inv(DevView v, const FftSysD
     const int cc = min(Kh, scr / ldq);
     for (int c0 = 0; c0 < Kh; c0 += cc) {
         int ldr;
-        line_fft<C, true>(Q + c0 * ldq, ldq, Q + c0 * ldq, ldq, A, B, ldq, K1, min(cc, Kh - c0), F.rad[1], F.np[1],
-                          twy, &ldr);
+        line_fft<C, true>(Q + c0 * ldq, ldq, Q + c0 * ldq, ldq, A, B, ldq, K1, min(cc, Kh - c0), F.ax[1], twy,
+                          &ldr);
     }
     T *out = static_cast<T *>(v.grid_real) + F.roff + (long long)x * K1 * K2;
     const int npairs = (K1 + 1) >> 1, zc = min(npairs, scr / ldz);
@@ -427,7 +427,7 @@ __global__ void __launch_bounds__(256) k_fft_y(DevView v, const FftSysDev *fs, c
         });
     __syncthreads();
     int ldr;
-    C *res = line_fft<C, INV>(a, ld, nullptr, 0, b, a, ld, n, nc, F.rad[1], F.np[1], tw, &ldr);
+    C *res = line_fft<C, INV>(a, ld, nullptr, 0, b, a, ld, n, nc, F.ax[1], tw, &ldr);
     for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
         int y = quot(e, inv_c), c = e - y * nc;
         g[(long long)y * Kh + c] = res[c * ldr + y];
@@ -466,7 +466,7 @@ __global__ void __launch_bounds__(256) k_fft_x_conv(DevView v, const FftSysDev *
         });
     __syncthreads();
     int ldr;
-    C *res = line_fft<C, false>(a, ld, nullptr, 0, b, a, ld, n, nc, F.rad[0], F.np[0], tw, &ldr);
+    C *res = line_fft<C, false>(a, ld, nullptr, 0, b, a, ld, n, nc, F.ax[0], tw, &ldr);
     C *other = res == a ? b : a;
     const ET *et = static_cast<const ET *>(v.eterm) + F.coff + (long long)y * Kh + z0;
     // the energy in fixed point per element: its sum is the same whatever
@@ -491,7 +491,7 @@ __global__ void __launch_bounds__(256) k_fft_x_conv(DevView v, const FftSysDev *
             res[c * ldr + kx] = Cx<C>::mk(s.x * f, s.y * f);
         });
     __syncthreads();
-    C *fin = line_fft<C, true>(res, ldr, nullptr, 0, other, res, ld, n, nc, F.rad[0], F.np[0], tw, &ldr);
+    C *fin = line_fft<C, true>(res, ldr, nullptr, 0, other, res, ld, n, nc, F.ax[0], tw, &ldr);
     for (int e = threadIdx.x; e < n * nc; e += blockDim.x) {
         int x = quot(e, inv_c), c = e - x * nc;
         g[x * xstride + c] = fin[c * ldr + x];
@@ -549,13 +549,24 @@ size_t fft_line_smem(int lines, int kmax, size_t csz) {
     return ((size_t)kmax + 2 * (size_t)lines * (size_t)(kmax | 1)) * csz;
 }
 
-static void factor(int n, int *rad, int *np) {
-    int k = 0;
-    while (n % 4 == 0) { rad[k++] = 4; n /= 4; }
-    while (n % 2 == 0) { rad[k++] = 2; n /= 2; }
-    while (n % 3 == 0) { rad[k++] = 3; n /= 3; }
-    while (n % 5 == 0) { rad[k++] = 5; n /= 5; }
-    *np = k;
+void fft_passes(int n, FftPasses &P) {
+    P = FftPasses{};
+    int k = 0, rest = n;
+    for (int r : {4, 2, 3, 5})
+        while (rest % r == 0 && k < kMaxPasses) {
+            P.R[k++] = r;
+            rest /= r;
+        }
+    P.np = k;
+    int Ns = 1;
+    for (int p = 0; p < k; ++p) {
+        P.Ns[p] = Ns;
+        P.m[p] = n / P.R[p];
+        P.step[p] = n / (Ns * P.R[p]);
+        P.inv_m[p] = 1.0f / (float)P.m[p];
+        P.inv_ns[p] = 1.0f / (float)Ns;
+        Ns *= P.R[p];
+    }
 }
 
 // Raises a kernel's dynamic shared-memory limit.  The limit is a per-kernel
@@ -596,7 +607,7 @@ void fft_plan_build(FftPlan &p, int mixed) {
     for (int s = 0; s < p.S; ++s) {
         FftSysDev &F = p.hsys[s];
         for (int d = 0; d < 3; ++d) {
-            factor(F.K[d], F.rad[d], &F.np[d]);
+            fft_passes(F.K[d], F.ax[d]);
             if (F.K[d] > p.kmax) p.kmax = F.K[d];
         }
         int nzb = (F.K[0] * F.K[1] + p.zlines - 1) / p.zlines;

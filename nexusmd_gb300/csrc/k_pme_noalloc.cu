@@ -300,16 +300,6 @@ bool smooth235(int n) {
     return n == 1;
 }
 
-// Stockham radices of one axis in the order the engine's FFT plan uses.
-void radices(int n, int *rad, int *np) {
-    int k = 0;
-    while (n % 4 == 0) { rad[k++] = 4; n /= 4; }
-    while (n % 2 == 0) { rad[k++] = 2; n /= 2; }
-    while (n % 3 == 0) { rad[k++] = 3; n /= 3; }
-    while (n % 5 == 0) { rad[k++] = 5; n /= 5; }
-    *np = k;
-}
-
 // Device address of g_pme_scratch on the current device, looked up once.
 int scratch_for_current_device(unsigned char **out) {
     int dev = -1;
@@ -369,7 +359,7 @@ extern "C" int nxm_pme_reciprocal_noalloc(const double *xyz, const double *charg
         F.K[d] = g.K[d];
         F.tw[d] = tw;
         tw += g.K[d];
-        radices(g.K[d], F.rad[d], &F.np[d]);
+        fft_passes(g.K[d], F.ax[d]);
     }
     F.Kh = g.Kh;
     FftPlan plan;  // geometry only; every pointer is into g_pme_scratch

@@ -9,6 +9,19 @@ namespace nxm {
 
 constexpr int kMaxPasses = 12;
 
+// The Stockham passes of one axis of length n, each pass's constants worked
+// out on the host: radix R, sub-transform size Ns before the pass,
+// butterflies per line m = n / R, twiddle stride n / (Ns R), and the FP32
+// reciprocals of m and Ns that the passes divide by.
+struct FftPasses {
+    int np;
+    int R[kMaxPasses], Ns[kMaxPasses], m[kMaxPasses], step[kMaxPasses];
+    float inv_m[kMaxPasses], inv_ns[kMaxPasses];
+};
+
+// Factors n = 2^a 3^b 5^c into passes of radix 4, 2, 3, 5 (in that order).
+void fft_passes(int n, FftPasses &P);
+
 // Per-system FFT geometry.  The real grid is row-major K0 x K1 x K2 (z
 // fastest, NonbondedForce.cpp:253); the half spectrum is K0 x K1 x Kh with
 // Kh = K2/2 + 1.
@@ -18,9 +31,7 @@ struct FftSysDev {
     long long roff;     // real grid offset (elements)
     long long coff;     // half-spectrum offset (elements)
     int tw[3];          // twiddle-table offset for the length of each axis
-    int np[3];          // Stockham passes per axis
-    int rad[3][kMaxPasses];
-    double wscale;      // unused padding for alignment
+    FftPasses ax[3];    // passes per axis
 };
 
 struct FftWork {
