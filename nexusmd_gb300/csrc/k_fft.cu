@@ -214,6 +214,25 @@ __device__ __forceinline__ void load_tw(C *dst, const DevView &v, int off, int n
     for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
 }
 
+// One spectrum element's reciprocal energy f |s|^2 (halved for an element
+// the half spectrum holds once) in fixed point, units of 1 / kEnergyScale.
+// FP64 engine: in FP64.  Mixed: in FP32, and converted without the FP64 pipe
+// (narrow on this GPU): a = e * 2^8 splits exactly into the integer-valued
+// h = rint(a) and l = a - h in [-1/2, 1/2], so round(e * 2^28) =
+// h * 2^20 + round(l * 2^20), valid for |e| < 2^23.
+__device__ __forceinline__ long long element_energy(double f, double2 s, bool once) {
+    const double wgt = once ? 0.5 * kEnergyScale : kEnergyScale;
+    return __double2ll_rn(wgt * f * (s.x * s.x + s.y * s.y));
+}
+__device__ __forceinline__ long long element_energy(float f, float2 s, bool once) {
+    static_assert(kEnergyScale == 268435456.0, "the split below assumes units of 2^-28");
+    const float e = (once ? 0.5f : 1.0f) * f * fmaf(s.x, s.x, s.y * s.y);
+    const float a = e * 256.0f;
+    const float h = rintf(a);
+    const float l = a - h;
+    return ((long long)__float2int_rn(h) << 20) + (long long)__float2int_rn(l * 1048576.0f);
+}
+
 // ---- z forward on nc real line pairs: line pair p (real lines ya = 2p and
 // ya + 1 of `acc`, row length K2; the second may not exist) becomes one
 // complex line, and after the transform they are separated with
@@ -485,8 +504,8 @@ __global__ void __launch_bounds__(256) k_fft_x_conv(DevView v, const FftSysDev *
             if (energy) {
                 // half spectrum: planes kz = 0 and kz = K2/2 (even K2) appear
                 // once; E = sum / 2
-                double wgt = (kz == 0 || 2 * kz == F.K[2]) ? 0.5 * kEnergyScale : kEnergyScale;
-                esum += __double2ll_rn(wgt * (double)f * ((double)s.x * (double)s.x + (double)s.y * (double)s.y));
+                const bool once = kz == 0 || 2 * kz == F.K[2];
+                esum += element_energy(f, s, once);
             }
             res[c * ldr + kx] = Cx<C>::mk(s.x * f, s.y * f);
         });

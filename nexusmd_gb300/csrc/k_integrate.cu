@@ -34,14 +34,29 @@ __global__ void __launch_bounds__(256) k_integrate(DevView v, double dt, int rep
         if (report) {
             int o = v.orig[s];
             double m = v.mass[s];
-            double vh[3] = {u[0], u[1], u[2]};
-            if (m > 0) {
-                double invMass = 1.0 / m;
-                double half = 0.5 * dt;
+            if (v.mixed) {
+                // the same estimate in FP32 from the stored 1/m (the FP64 pipe is
+                // narrow on this GPU); the force word converts exactly in two parts
+                float vh[3];
+                const float kf = m > 0 ? (float)(v.invm[s] * (0.5 * dt)) : 0.0f;
 #pragma unroll
-                for (int c = 0; c < 3; ++c) vh[c] += F(c) * invMass * half;
+                for (int c = 0; c < 3; ++c) {
+                    const long long wc = static_cast<long long>(w[c]);
+                    const float fc = __int2float_rn((int)(wc >> 24)) * 0.00390625f +                   // 2^-8
+                                     __uint2float_rn((unsigned)(wc & 0xffffff)) * 2.3283064365386963e-10f;  // 2^-32
+                    vh[c] = fmaf(fc, kf, (float)u[c]);
+                }
+                ke = (double)(0.5f * (float)m * fmaf(vh[0], vh[0], fmaf(vh[1], vh[1], vh[2] * vh[2])));
+            } else {
+                double vh[3] = {u[0], u[1], u[2]};
+                if (m > 0) {
+                    double invMass = 1.0 / m;
+                    double half = 0.5 * dt;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) vh[c] += F(c) * invMass * half;
+                }
+                ke = 0.5 * m * (vh[0] * vh[0] + vh[1] * vh[1] + vh[2] * vh[2]);
             }
-            ke = 0.5 * m * (vh[0] * vh[0] + vh[1] * vh[1] + vh[2] * vh[2]);
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 v.snap_x[3 * (size_t)o + c] = p[c];
