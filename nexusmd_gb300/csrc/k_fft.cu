@@ -656,16 +656,25 @@ void fft_plan_build(FftPlan &p, int mixed) {
     p.plane_ok = p.S > 0 && p.scr >= minscr;
     if (!p.plane_ok) p.plane = 0;
     p.smem_plane = ((size_t)p.twcap + p.qcap + 2 * (size_t)std::max(p.scr, 0)) * csz;
-    cudaMalloc(&p.dsys, sizeof(FftSysDev) * p.S);
+    // device buffers are kept across rebuilds of the same plan (the autotuner
+    // rebuilds it per candidate) and grown when too small
+    auto ensure = [](auto *&ptr, size_t &cap, size_t n) {
+        if (n <= cap && ptr) return;
+        cudaFree(ptr);
+        ptr = nullptr;
+        cudaMalloc(&ptr, sizeof(*ptr) * n);
+        cap = n;
+    };
+    ensure(p.dsys, p.cap[0], (size_t)std::max(p.S, 1));
     cudaMemcpy(p.dsys, p.hsys.data(), sizeof(FftSysDev) * p.S, cudaMemcpyHostToDevice);
     p.nz = (int)z.size();
     p.ny = (int)y.size();
     p.nx = (int)x.size();
     p.npl = (int)pl.size();
-    cudaMalloc(&p.zwork, sizeof(FftWork) * (p.nz + 1));
-    cudaMalloc(&p.ywork, sizeof(FftWork) * (p.ny + 1));
-    cudaMalloc(&p.xwork, sizeof(FftWork) * (p.nx + 1));
-    cudaMalloc(&p.pwork, sizeof(FftWork) * (p.npl + 1));
+    ensure(p.zwork, p.cap[1], (size_t)p.nz + 1);
+    ensure(p.ywork, p.cap[2], (size_t)p.ny + 1);
+    ensure(p.xwork, p.cap[3], (size_t)p.nx + 1);
+    ensure(p.pwork, p.cap[4], (size_t)p.npl + 1);
     cudaMemcpy(p.zwork, z.data(), sizeof(FftWork) * p.nz, cudaMemcpyHostToDevice);
     cudaMemcpy(p.ywork, y.data(), sizeof(FftWork) * p.ny, cudaMemcpyHostToDevice);
     cudaMemcpy(p.xwork, x.data(), sizeof(FftWork) * p.nx, cudaMemcpyHostToDevice);
@@ -682,6 +691,7 @@ void fft_plan_free(FftPlan &p) {
     cudaFree(p.ywork);
     cudaFree(p.xwork);
     cudaFree(p.pwork);
+    for (size_t &c : p.cap) c = 0;
     p.dsys = nullptr;
     p.zwork = p.ywork = p.xwork = p.pwork = nullptr;
 }

@@ -723,7 +723,6 @@ std::string Engine::autotune() {
     for (int cols : {4, 8, 16}) {
         for (int zl : {8, 16, 32}) {
             if (!try_line && zl != 16) continue;  // the z blocking is unused on the plane path
-            fft_plan_free(plan_);
             plan_.zlines = zl;
             plan_.cols = cols;
             fft_plan_build(plan_, mixed_);
@@ -745,7 +744,6 @@ std::string Engine::autotune() {
             }
         }
     }
-    fft_plan_free(plan_);
     plan_.zlines = bz;
     plan_.cols = bc;
     fft_plan_build(plan_, mixed_);

@@ -44,6 +44,7 @@ struct FftPlan {
     FftSysDev *dsys = nullptr;
     std::vector<FftSysDev> hsys;
     FftWork *zwork = nullptr, *ywork = nullptr, *xwork = nullptr;
+    size_t cap[5] = {};   // allocated elements of dsys, zwork, ywork, xwork, pwork
     int nz = 0, ny = 0, nx = 0;
     int zlines = 16;    // real lines per block in the z passes (even)
     int cols = 8;       // z columns per block in the y and x passes

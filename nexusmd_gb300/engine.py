@@ -119,14 +119,15 @@ class Engine:
     def __init__(self, systems, precision=PRECISION_MIXED, skin=0.1, rebuild_interval=10,
                  force_mask=FORCE_ALL, box="reference", grid=None, use_switch=0,
                  switch_dist=0.0, exclusion_depth=3, max_neighbors=0, device=0, exceptions=False,
-                 fft_path=0):
+                 fft_path=0, autotune=True):
         """``box``: "reference" (extent + 1%, as the reference) or "explicit"
         (each system's periodic box [0, L)); ``grid``: None = each system's
         ``grid`` attribute, (0,0,0) = the reference's power-of-two rule;
         ``exceptions``: pass each system's ``exc_idx`` / ``exc_prm`` exception
         pairs (OpenMM semantics) when it has them; ``fft_path``: PME FFT
         launch shape, 0 = autotuned, 1 = line path, 2 = plane path where the
-        x-planes fit in shared memory."""
+        x-planes fit in shared memory; ``autotune``: time the launch shapes
+        that change no result at creation and keep the fastest."""
         L = load_library()
         if not isinstance(systems, (list, tuple)):
             systems = [systems]
@@ -173,7 +174,7 @@ class Engine:
         L.nxm_default_options(C.byref(opt))
         opt.precision, opt.skin, opt.rebuild_interval = int(precision), float(skin), int(rebuild_interval)
         opt.device, opt.max_neighbors = int(device), int(max_neighbors)
-        opt.fft_path = int(fft_path)
+        opt.fft_path, opt.autotune = int(fft_path), 1 if autotune else 0
         h = C.c_void_p()
         _check(L.nxm_create(descs, len(systems), C.byref(opt), np.concatenate(pos), C.byref(h)),
                "nxm_create")
