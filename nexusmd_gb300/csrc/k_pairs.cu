@@ -393,7 +393,7 @@ __device__ __forceinline__ float2 erfcx_fit2(float2 t) {
 template <bool ENERGY>
 __device__ __forceinline__ void pair_mixed2(bool in0, bool in1, float2 dxy0, float dz0, float2 dxy1, float dz1,
                                             float2 r2, float2 qq, float2 sg, float2 eps, const PairPrm2 &P,
-                                            float2 &fxy, float &fz, float &ec, float &ev) {
+                                            float2 &fxy, float &fz, float2 &ecv) {
     float2 rinv = make_float2(fast_rsqrt(r2.x), fast_rsqrt(r2.y));
     float2 rinv2 = __fmul2_rn(rinv, rinv);
     float2 r = __fmul2_rn(r2, rinv);
@@ -405,6 +405,7 @@ __device__ __forceinline__ void pair_mixed2(bool in0, bool in1, float2 dxy0, flo
     float2 dEdR = __fmul2_rn(__fmul2_rn(qr, rinv2), __ffma2_rn(__fmul2_rn(P.k2a, r), ex, erfcv));
     float2 s2 = __fmul2_rn(__fmul2_rn(sg, sg), rinv2);
     float2 s6 = __fmul2_rn(__fmul2_rn(s2, s2), s2);
+
     float2 lj = __fmul2_rn(__fmul2_rn(eps, __ffma2_rn(P.twelve, s6, P.msix)), s6);
     dEdR = __ffma2_rn(lj, rinv2, dEdR);
     const float d0 = in0 ? dEdR.x : 0.0f, d1 = in1 ? dEdR.y : 0.0f;
@@ -413,12 +414,12 @@ __device__ __forceinline__ void pair_mixed2(bool in0, bool in1, float2 dxy0, flo
     fxy = __ffma2_rn(dxy1, dup2(d1), fxy);
     fz = fmaf(dz1, d1, fz);
     if (ENERGY) {
-        float2 e = __fmul2_rn(qr, erfcv);
-        float2 evdw = __fmul2_rn(__fmul2_rn(eps, __fadd2_rn(s6, P.mone)), s6);
-        ec += in0 ? e.x : 0.0f;
-        ev += in0 ? evdw.x : 0.0f;
-        ec += in1 ? e.y : 0.0f;
-        ev += in1 ? evdw.y : 0.0f;
+        // (Coulomb, LJ) as one packed sum, entry 0 then entry 1 (entries
+        // outside the cutoff add zero)
+        const float2 e = __fmul2_rn(qr, erfcv);
+        const float2 l = __fmul2_rn(__fmul2_rn(eps, __fadd2_rn(s6, P.mone)), s6);
+        ecv = __fadd2_rn(ecv, make_float2(in0 ? e.x : 0.0f, in0 ? l.x : 0.0f));
+        ecv = __fadd2_rn(ecv, make_float2(in1 ? e.y : 0.0f, in1 ? l.y : 0.0f));
     }
 }
 
@@ -463,6 +464,7 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_pairs_mixed(DevView v) {
     const PairPrm2 P2{dup2(S.ex2c), dup2(S.a04), dup2(S.k2a), dup2(1.0f), dup2(12.0f), dup2(-6.0f), dup2(-1.0f)};
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     float ec = 0.f, ev = 0.f;
+    float2 ecv = make_float2(0.f, 0.f);  // pair_mixed2's (Coulomb, LJ) sums
     for (int i = a0 + warp; i < a1; i += nw) {
         float pi3[3];
         i_in_group_frame(v, S, i, czf, pi3);
@@ -515,7 +517,7 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_pairs_mixed(DevView v) {
                     } else {
                         pair_mixed2<ENERGY>(in0, in1, dxy0, dz0, dxy1, dz1, make_float2(r20, r21),
                                             make_float2(qi * p0.w, qi * p1.w), make_float2(li.x + l0.x, li.x + l1.x),
-                                            make_float2(li.y * l0.y, li.y * l1.y), P2, fxy, fz, ec, ev);
+                                            make_float2(li.y * l0.y, li.y * l1.y), P2, fxy, fz, ecv);
                     }
                 }
             };
@@ -540,6 +542,10 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_pairs_mixed(DevView v) {
         }
     }
     if (ENERGY) {
+        if (!SW) {
+            ec = ecv.x;
+            ev = ecv.y;
+        }
         // each pair sits in both partners' lists
         energy_add(v.E, G.sys, E_COUL, 0.5 * (double)ec);
         energy_add(v.E, G.sys, E_VDW, 0.5 * (double)ev);
