@@ -125,14 +125,21 @@ __global__ void __launch_bounds__(kSpreadWarps * 32) k_spread_warp(DevView v, co
                 const FftSysDev &F = fs[sys];
                 int idx[3];
                 float fr[3];
+                // grid coordinate = the atom's cell corner's (a table built in
+                // FP64 on the host) + the FP32 offset in the cell times K / L:
+                // no FP64 arithmetic, which is narrow on this GPU
+                const float4 pq = v.pf[s];
+                const float po[3] = {pq.x, pq.y, pq.z};
+                const int c3 = v.cell3[s];
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
-                    double p = d == 0 ? v.x[s] : d == 1 ? v.y[s] : v.z[s];
-                    double t = p * S.invL[d];
-                    t = (t - floor(t)) * F.K[d];
-                    int ti = (int)t;
-                    fr[d] = (float)(t - ti);
-                    idx[d] = ti % F.K[d];
+                    const float2 cg = v.cgrid[S.cg_off[d] + ((c3 >> (10 * d)) & 1023)];
+                    const float u = fmaf(po[d], S.kl[d], cg.y);
+                    const float fl = floorf(u);
+                    int ti = ((int)cg.x + (int)fl) % F.K[d];  // a cell spans several grid points
+                    ti += ti < 0 ? F.K[d] : 0;
+                    fr[d] = u - fl;
+                    idx[d] = ti;
                     s_i[warp][lane][d] = idx[d];
                 }
                 v.pme_idx[s] = make_int4(idx[0], idx[1], idx[2], 0);

@@ -79,6 +79,11 @@ struct SysDev {
     // FP32 pair-kernel constants: exp(-(alpha r)^2) = 2^(r^2 ex2c),
     // 0.4 alpha (erfc fit argument), 2 alpha / sqrt(pi); cell edges
     float ex2c, a04, k2a, csf[3];
+    // PME grid coordinates from cell-relative positions (mixed precision):
+    // cgrid[cg_off[d] + c] holds the grid coordinate of cell c's lower corner
+    // along axis d (integer part, fraction); kl = K / L
+    int cg_off[3];
+    float kl[3];
 };
 
 // Flags word layout in device memory.

@@ -206,7 +206,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     std::vector<int2> ex_pairs;
     std::vector<int2> xc_pairs;      // exception pairs, batch-global original indices
     std::vector<double4> xc_prm;
-    int off = 0, cell_off = 0;
+    int off = 0, cell_off = 0, cg_total = 0;
     long long roff = 0, coff = 0;
     int tw_total = 0;
     double skin = opt.skin > 0 ? opt.skin : 0.0;
@@ -286,6 +286,11 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         D.cgrid_off = coff;
         D.cell_off = cell_off;
         cell_off += D.nc[0] * D.nc[1] * D.nc[2];
+        for (int d = 0; d < 3; ++d) {
+            D.cg_off[d] = cg_total;
+            cg_total += D.nc[d];
+            D.kl[d] = (float)((double)H.K[d] * D.invL[d]);
+        }
 
         FftSysDev &F = plan_.hsys[s];
         for (int d = 0; d < 3; ++d) F.K[d] = H.K[d];
@@ -477,6 +482,24 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
                                     (float)(-oz * sysd_[s].cs[2]), 0.f);
                 }
     up(v_.dtab, dt.data(), sizeof(float4) * dt.size());
+
+    // PME grid coordinate of every cell's lower corner, per axis, as the
+    // reference forms a particle's (t = frac(x / L) K, NonbondedForce.cpp:51-71)
+    {
+        std::vector<float2> cg(std::max(cg_total, 1), make_float2(0.f, 0.f));
+        for (int s = 0; s < S; ++s) {
+            const SysDev &D = sysd_[s];
+            for (int d = 0; d < 3; ++d)
+                for (int c = 0; c < D.nc[d]; ++c) {
+                    double t = (D.lb[d] + c * D.cs[d]) * D.invL[d];
+                    t = (t - std::floor(t)) * D.K[d];
+                    int ti = std::min((int)t, D.K[d] - 1);
+                    cg[(size_t)D.cg_off[d] + c] = make_float2((float)ti, (float)(t - ti));
+                }
+        }
+        v_.cgrid = dalloc<float2>(cg.size());
+        up(v_.cgrid, cg.data(), sizeof(float2) * cg.size());
+    }
 
     // exclusion CSR (batch-global original indices)
     std::vector<int> eoff(N_ + 1, 0), elst;

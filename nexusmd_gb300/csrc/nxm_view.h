@@ -51,6 +51,7 @@ struct DevView {
     int *gspan;          // [ngroups][kGroupSpanWords]: each group's neighbourhood spans, written by the list build
     int2 *gspan_n;       // [ngroups]: (atoms, spans) of that neighbourhood
     float4 *dtab;        // [S][kDtabStride] cell-image displacement per code
+    float2 *cgrid;       // per system and axis, per cell: corner's PME grid coordinate (int part, fraction)
     double *xref;        // [3][N] positions at the last rebuild
     float4 *oref;        // mixed: cell offsets at the last rebuild, .w = q * sqrt(ke)
     int *excl_off, *excl_lst;  // CSR by original index, partners as original indices
