@@ -246,10 +246,15 @@ __global__ void __launch_bounds__(256) k_gather(DevView v, const FftSysDev *fs) 
         }
     }
     R q = (R)v.q[s];
+    // K / L per axis: precomputed in FP32 for the mixed engine (the same
+    // rounding of the same FP64 product), in FP64 otherwise
+    R kl[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) kl[d] = sizeof(R) == 4 ? (R)S.kl[d] : (R)(F.K[d] * S.invL[d]);
     using Acc_ = Acc;
-    acc_add(static_cast<Acc_ *>(v.fx) + s, -(q * (fx * (R)(F.K[0] * S.invL[0]))));
-    acc_add(static_cast<Acc_ *>(v.fy) + s, -(q * (fy * (R)(F.K[1] * S.invL[1]))));
-    acc_add(static_cast<Acc_ *>(v.fz) + s, -(q * (fz * (R)(F.K[2] * S.invL[2]))));
+    acc_add(static_cast<Acc_ *>(v.fx) + s, -(q * (fx * kl[0])));
+    acc_add(static_cast<Acc_ *>(v.fy) + s, -(q * (fy * kl[1])));
+    acc_add(static_cast<Acc_ *>(v.fz) + s, -(q * (fz * kl[2])));
 }
 
 // Spread: bound by the L2 atomics (125 int64 per atom), and by how many
