@@ -33,31 +33,63 @@ struct Cx;
 template <>
 struct Cx<float2> {
     using R = float;
-    static __device__ __forceinline__ float2 mk(float a, float b) { return make_float2(a, b); }
+    static __host__ __device__ __forceinline__ float2 mk(float a, float b) { return make_float2(a, b); }
 };
 template <>
 struct Cx<double2> {
     using R = double;
-    static __device__ __forceinline__ double2 mk(double a, double b) { return make_double2(a, b); }
+    static __host__ __device__ __forceinline__ double2 mk(double a, double b) { return make_double2(a, b); }
 };
 
 template <typename C>
-__device__ __forceinline__ C cadd(C a, C b) { return Cx<C>::mk(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ C cadd(C a, C b) { return Cx<C>::mk(a.x + b.x, a.y + b.y); }
 template <typename C>
-__device__ __forceinline__ C csub(C a, C b) { return Cx<C>::mk(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ C csub(C a, C b) { return Cx<C>::mk(a.x - b.x, a.y - b.y); }
 template <typename C>
-__device__ __forceinline__ C cmul(C a, C b) { return Cx<C>::mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__host__ __device__ __forceinline__ C cmul(C a, C b) { return Cx<C>::mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 // i * s * a
 template <typename C>
-__device__ __forceinline__ C cis(C a, typename Cx<C>::R s) { return Cx<C>::mk(-s * a.y, s * a.x); }
+__host__ __device__ __forceinline__ C cis(C a, typename Cx<C>::R s) { return Cx<C>::mk(-s * a.y, s * a.x); }
 template <typename C>
-__device__ __forceinline__ C cscale(C a, typename Cx<C>::R s) { return Cx<C>::mk(a.x * s, a.y * s); }
+__host__ __device__ __forceinline__ C cscale(C a, typename Cx<C>::R s) { return Cx<C>::mk(a.x * s, a.y * s); }
 
-// Length-R DFT with root exp(sign * 2 pi i / R), R in {2, 3, 4, 5}.
+// Length-R DFT with root exp(sign * 2 pi i / R), R in {2, 3, 4, 5, 8, 10}:
+// 2, 3, 4, 5 directly; 8 and 10 as two DFTs of half the length on the even
+// and odd inputs, the odd ones twiddled by exp(sign * 2 pi i k / R), then R/2
+// DFTs of length 2 (one pass in registers instead of two through shared
+// memory).
 template <typename C, int R>
-__device__ __forceinline__ void small_dft(C *v, typename Cx<C>::R s) {
+__host__ __device__ __forceinline__ void small_dft(C *v, typename Cx<C>::R s) {
     using T = typename Cx<C>::R;
-    if (R == 2) {
+    if constexpr (R == 8 || R == 10) {
+        constexpr int H = R / 2;
+        C e[H], o[H];
+#pragma unroll
+        for (int k = 0; k < H; ++k) {
+            e[k] = v[2 * k];
+            o[k] = v[2 * k + 1];
+        }
+        small_dft<C, H>(e, s);
+        small_dft<C, H>(o, s);
+        if constexpr (R == 8) {
+            const T h = (T)0.70710678118654752440;  // sqrt(2)/2
+            o[1] = cmul(o[1], Cx<C>::mk(h, s * h));
+            o[2] = cis(o[2], s);
+            o[3] = cmul(o[3], Cx<C>::mk(-h, s * h));
+        } else {
+            const T c1 = (T)0.80901699437494742410, s1 = (T)0.58778525229247312917;  // 36 degrees
+            const T c2 = (T)0.30901699437494742410, s2 = (T)0.95105651629515357212;  // 72 degrees
+            o[1] = cmul(o[1], Cx<C>::mk(c1, s * s1));
+            o[2] = cmul(o[2], Cx<C>::mk(c2, s * s2));
+            o[3] = cmul(o[3], Cx<C>::mk(-c2, s * s2));
+            o[4] = cmul(o[4], Cx<C>::mk(-c1, s * s1));
+        }
+#pragma unroll
+        for (int k = 0; k < H; ++k) {
+            v[k] = cadd(e[k], o[k]);
+            v[k + H] = csub(e[k], o[k]);
+        }
+    } else if (R == 2) {
         C a = v[0], b = v[1];
         v[0] = cadd(a, b);
         v[1] = csub(a, b);
@@ -114,7 +146,7 @@ __device__ __forceinline__ void stockham(const C *src, int lds, C *dst, int ldd,
         int l = quot(bi, inv_m), j = bi - l * m;
         int jq = quot(j, inv_ns), k = j - jq * Ns;
         const C *s = src + l * lds + j;
-        C v[5];
+        C v[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) v[r] = s[r * m];
         if (k) {
@@ -153,6 +185,8 @@ __device__ C *line_fft(C *in, int ldi, C *out, int ldo, C *s0, C *s1, int lds, i
             ld = ldo;
         }
         switch (P.R[p]) {
+            case 10: stockham<C, 10, INV>(src, ls, dst, ld, nl, P, p, tw); break;
+            case 8: stockham<C, 8, INV>(src, ls, dst, ld, nl, P, p, tw); break;
             case 4: stockham<C, 4, INV>(src, ls, dst, ld, nl, P, p, tw); break;
             case 2: stockham<C, 2, INV>(src, ls, dst, ld, nl, P, p, tw); break;
             case 3: stockham<C, 3, INV>(src, ls, dst, ld, nl, P, p, tw); break;
@@ -571,7 +605,7 @@ size_t fft_line_smem(int lines, int kmax, size_t csz) {
 void fft_passes(int n, FftPasses &P) {
     P = FftPasses{};
     int k = 0, rest = n;
-    for (int r : {4, 2, 3, 5})
+    for (int r : {10, 8, 4, 2, 3, 5})
         while (rest % r == 0 && k < kMaxPasses) {
             P.R[k++] = r;
             rest /= r;

@@ -19,7 +19,8 @@ struct FftPasses {
     float inv_m[kMaxPasses], inv_ns[kMaxPasses];
 };
 
-// Factors n = 2^a 3^b 5^c into passes of radix 4, 2, 3, 5 (in that order).
+// Factors n = 2^a 3^b 5^c into passes of radix 10, 8, 4, 2, 3, 5 (the
+// larger first: fewer passes through shared memory).
 void fft_passes(int n, FftPasses &P);
 
 // Per-system FFT geometry.  The real grid is row-major K0 x K1 x K2 (z
