@@ -53,15 +53,38 @@ __host__ __device__ __forceinline__ C cis(C a, typename Cx<C>::R s) { return Cx<
 template <typename C>
 __host__ __device__ __forceinline__ C cscale(C a, typename Cx<C>::R s) { return Cx<C>::mk(a.x * s, a.y * s); }
 
-// Length-R DFT with root exp(sign * 2 pi i / R), R in {2, 3, 4, 5, 8, 10}:
-// 2, 3, 4, 5 directly; 8 and 10 as two DFTs of half the length on the even
-// and odd inputs, the odd ones twiddled by exp(sign * 2 pi i k / R), then R/2
-// DFTs of length 2 (one pass in registers instead of two through shared
-// memory).
+// Length-R DFT with root exp(sign * 2 pi i / R), R in {2, 3, 4, 5, 6, 8, 9,
+// 10}: 2, 3, 4, 5 directly; 6, 8 and 10 as two DFTs of half the length on the
+// even and odd inputs, the odd ones twiddled by exp(sign * 2 pi i k / R), then
+// R/2 DFTs of length 2; 9 as three DFTs of length 3 on the inputs n = n1 mod
+// 3, twiddled by exp(sign * 2 pi i n1 k / 9), then three DFTs of length 3 --
+// one pass in registers instead of two through shared memory.
 template <typename C, int R>
 __host__ __device__ __forceinline__ void small_dft(C *v, typename Cx<C>::R s) {
     using T = typename Cx<C>::R;
-    if constexpr (R == 8 || R == 10) {
+    if constexpr (R == 9) {
+        const T c1 = (T)0.76604444311897803520, s1 = (T)0.64278760968653932632;   // 40 degrees
+        const T c2 = (T)0.17364817766693034885, s2 = (T)0.98480775301220805936;   // 80 degrees
+        const T c4 = (T)-0.93969262078590838405, s4 = (T)0.34202014332566873304;  // 160 degrees
+        C y[3][3];
+#pragma unroll
+        for (int g = 0; g < 3; ++g) {
+#pragma unroll
+            for (int j = 0; j < 3; ++j) y[g][j] = v[g + 3 * j];
+            small_dft<C, 3>(y[g], s);
+        }
+        y[1][1] = cmul(y[1][1], Cx<C>::mk(c1, s * s1));
+        y[1][2] = cmul(y[1][2], Cx<C>::mk(c2, s * s2));
+        y[2][1] = cmul(y[2][1], Cx<C>::mk(c2, s * s2));
+        y[2][2] = cmul(y[2][2], Cx<C>::mk(c4, s * s4));
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            C z[3] = {y[0][k], y[1][k], y[2][k]};
+            small_dft<C, 3>(z, s);
+#pragma unroll
+            for (int j = 0; j < 3; ++j) v[k + 3 * j] = z[j];
+        }
+    } else if constexpr (R == 6 || R == 8 || R == 10) {
         constexpr int H = R / 2;
         C e[H], o[H];
 #pragma unroll
@@ -71,7 +94,11 @@ __host__ __device__ __forceinline__ void small_dft(C *v, typename Cx<C>::R s) {
         }
         small_dft<C, H>(e, s);
         small_dft<C, H>(o, s);
-        if constexpr (R == 8) {
+        if constexpr (R == 6) {
+            const T h = (T)0.86602540378443864676;  // sqrt(3)/2
+            o[1] = cmul(o[1], Cx<C>::mk((T)0.5, s * h));
+            o[2] = cmul(o[2], Cx<C>::mk((T)-0.5, s * h));
+        } else if constexpr (R == 8) {
             const T h = (T)0.70710678118654752440;  // sqrt(2)/2
             o[1] = cmul(o[1], Cx<C>::mk(h, s * h));
             o[2] = cis(o[2], s);
@@ -186,6 +213,8 @@ __device__ C *line_fft(C *in, int ldi, C *out, int ldo, C *s0, C *s1, int lds, i
         }
         switch (P.R[p]) {
             case 10: stockham<C, 10, INV>(src, ls, dst, ld, nl, P, p, tw); break;
+            case 9: stockham<C, 9, INV>(src, ls, dst, ld, nl, P, p, tw); break;
+            case 6: stockham<C, 6, INV>(src, ls, dst, ld, nl, P, p, tw); break;
             case 8: stockham<C, 8, INV>(src, ls, dst, ld, nl, P, p, tw); break;
             case 4: stockham<C, 4, INV>(src, ls, dst, ld, nl, P, p, tw); break;
             case 2: stockham<C, 2, INV>(src, ls, dst, ld, nl, P, p, tw); break;
@@ -605,7 +634,7 @@ size_t fft_line_smem(int lines, int kmax, size_t csz) {
 void fft_passes(int n, FftPasses &P) {
     P = FftPasses{};
     int k = 0, rest = n;
-    for (int r : {10, 8, 4, 2, 3, 5})
+    for (int r : {10, 9, 8, 6, 4, 2, 3, 5})
         while (rest % r == 0 && k < kMaxPasses) {
             P.R[k++] = r;
             rest /= r;

@@ -19,7 +19,7 @@ struct FftPasses {
     float inv_m[kMaxPasses], inv_ns[kMaxPasses];
 };
 
-// Factors n = 2^a 3^b 5^c into passes of radix 10, 8, 4, 2, 3, 5 (the
+// Factors n = 2^a 3^b 5^c into passes of radix 10, 9, 8, 6, 4, 2, 3, 5 (the
 // larger first: fewer passes through shared memory).
 void fft_passes(int n, FftPasses &P);
 

@@ -47,8 +47,8 @@ static bool check_radix() {
 }
 
 int main() {
-    bool ok = check_radix<2>() && check_radix<3>() && check_radix<4>() && check_radix<5>() && check_radix<8>() &&
-              check_radix<10>();
+    bool ok = check_radix<2>() && check_radix<3>() && check_radix<4>() && check_radix<5>() && check_radix<6>() &&
+              check_radix<8>() && check_radix<9>() && check_radix<10>();
     int lengths = 0;
     for (int n = 1; n <= 1024; ++n) {
         int r = n;

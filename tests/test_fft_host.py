@@ -1,7 +1,7 @@
 """The FFT's register DFTs and plan factorisation, checked on the host.
 
 tests/host/fft_butterflies.cu includes the FFT source and runs its
-host-callable parts (the radix 2, 3, 4, 5, 8 and 10 DFTs, the pass
+host-callable parts (the radix 2, 3, 4, 5, 6, 8, 9 and 10 DFTs, the pass
 constants of every supported length) against the direct DFT; needs nvcc,
 no GPU.
 """
