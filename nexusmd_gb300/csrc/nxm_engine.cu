@@ -596,8 +596,6 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     for (auto &h : sysh_) any_nb |= (h.force_mask & NXM_FORCE_NONBONDED) != 0;
     v_.total_grid = roff;
     v_.total_cgrid = coff;
-    size_t rsz = mixed_ ? sizeof(float) : sizeof(double);
-    size_t csz = 2 * rsz;
     if (any_nb) {
         v_.grid_acc = mixed_ ? (void *)dalloc<long long>(roff) : (void *)dalloc<double>(roff);
         v_.grid_real = mixed_ ? (void *)dalloc<float>(roff) : (void *)dalloc<double>(roff);
@@ -605,7 +603,6 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         v_.eterm = mixed_ ? (void *)dalloc<float>(coff) : (void *)dalloc<double>(coff);
         v_.twiddle = mixed_ ? (void *)dalloc<float2>(tw_total) : (void *)dalloc<double2>(tw_total);
         if (!v_.grid_acc || !v_.grid_cplx) return "device allocation failed (PME grids)";
-        (void)csz;
         // twiddles exp(-2 pi i t / K)
         std::vector<double> tw(2 * (size_t)tw_total);
         for (int s = 0; s < S; ++s)
