@@ -13,6 +13,8 @@
 #include <queue>
 #include <string>
 
+#include <thread>
+
 #include "nxm_engine.h"
 
 namespace nxm {
@@ -634,7 +636,9 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
             int K0 = H.K[0], K1 = H.K[1], K2 = H.K[2], Kh = K2 / 2 + 1;
             int maxkx = (K0 + 1) / 2, maxky = (K1 + 1) / 2, maxkz = (K2 + 1) / 2;
             double *e = et.data() + plan_.hsys[s].coff;
-            for (int kx = 0; kx < K0; ++kx) {
+            // one x-plane per task over the host's threads: every element is
+            // computed on its own, so the values do not depend on the split
+            auto plane = [&](int kx) {
                 double mx = (kx < maxkx) ? kx : (kx - K0);
                 double mhx = mx * recip[0];
                 double bx = boxfactor * mod[0][kx];
@@ -656,7 +660,15 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
                         e[idx] = one_4pi_eps * std::exp(-factor * m2) / denom;
                     }
                 }
-            }
+            };
+            const int nth = std::max(1, std::min<int>(K0, (int)std::thread::hardware_concurrency()));
+            std::vector<std::thread> pool;
+            for (int t = 1; t < nth; ++t)
+                pool.emplace_back([&, t] {
+                    for (int kx = t; kx < K0; kx += nth) plane(kx);
+                });
+            for (int kx = 0; kx < K0; kx += nth) plane(kx);
+            for (auto &th : pool) th.join();
         }
         if (mixed_) {
             std::vector<float> ef(et.begin(), et.end());
