@@ -131,11 +131,6 @@ typedef struct nxm_ctx nxm_ctx;
 
 const char *nxm_version(void);
 
-/* FP32 fused multiply-add throughput of a device (TFLOP/s, 2 flops per FMA):
- * scalar FFMA and packed FP32x2 FFMA2, each the best of 5 timed launches of a
- * probe kernel that keeps every SM busy.  The roofline denominator of the
- * FP32-bound pair kernel.  Runs its own stream; no context needed. */
-int nxm_fp32_peak(int32_t device, double *tflops_scalar, double *tflops_packed);
 const char *nxm_last_error(void);
 void nxm_default_options(nxm_options *opt);
 
@@ -155,6 +150,24 @@ int nxm_compute_forces(nxm_ctx *ctx);
 /* nsteps leapfrog steps of dt ps.  Energies and the x/v/F snapshot are taken
  * on the last step (and the kinetic energy with them). */
 int nxm_step(nxm_ctx *ctx, int32_t nsteps, double dt);
+
+/* ---- Pipelined stepping with frames read back into pinned host memory
+ * (the reference's Engine::RunSimulation loop with Report, Engine.cpp:162-188,
+ * with the report copies overlapped with the next steps).
+ * nxm_frames_init: a ring of `depth` frame slots (1..64) in pinned host
+ * memory owned by the context; nxm_step_async makes a ring of 2 when none was
+ * made.  nxm_step_async: enqueues nsteps steps (the last computes energies and
+ * the snapshot) and copies of that step's positions (original atom order,
+ * [n][3]), energies and device flags into the next free slot, and returns
+ * without waiting; NXM_ERR_INVALID when every slot still holds a frame that
+ * nxm_frame_wait has not handed out.  nxm_frame_wait: waits for the oldest
+ * pending frame; *xyz (if xyz is not NULL) points at its positions, valid until
+ * the slot is filled again `depth` nxm_step_async calls later; energies of
+ * the first n_systems systems go to energies[]; device errors of the frame's
+ * steps are reported here. */
+int nxm_frames_init(nxm_ctx *ctx, int32_t depth);
+int nxm_step_async(nxm_ctx *ctx, int32_t nsteps, double dt);
+int nxm_frame_wait(nxm_ctx *ctx, const double **xyz, nxm_energies *energies, int32_t n_systems);
 
 /* Snapshot of the last force evaluation: positions and velocities as they
  * were when the forces were computed (before that step's update). */
@@ -201,6 +214,40 @@ int nxm_get_tuning(nxm_ctx *ctx, int32_t out[3]);
 /* Threads per block of the FFT's plane path (the autotuner's pick or the
  * default), or 0 when the FFT runs on the line path. */
 int nxm_get_fft_plane_threads(nxm_ctx *ctx, int32_t *threads);
+
+/* One system's PME grids from the last force evaluation, as doubles (any
+ * pointer may be NULL): the charge grid the spread summed, [K0][K1][K2]
+ * (gridSpreadCharge_Reference, NonbondedForce.cpp:220-260); the influence
+ * function on the half spectrum, [K0][K1][K2/2+1] (the eterm of
+ * reciprocalConvolutionAndEnergy, :323-388); and the real grid after the
+ * forward transform, the convolution and the unnormalised inverse transform,
+ * [K0][K1][K2] (what PMEGridForces reads, :407-461).  Waits for the
+ * context's work.  For checking the FFT against another implementation. */
+int nxm_get_pme_grids(nxm_ctx *ctx, int32_t system, double *charge, double *influence, double *potential);
+
+/* Host wall-clock milliseconds of the context's creation: [0] host set-up
+ * (box, per-system constants, exclusions), [1] device allocation and
+ * uploads, [2] PME tables (twiddles, B-spline moduli, influence function)
+ * and FFT plan, [3] autotuning of launch shapes (about 0 when autotune is
+ * off or an earlier context of the same shapes in this process was tuned:
+ * *autotune_cached = 1), [4] step-graph builds so far (the first steps
+ * build them), [5] the creation total [0] + [1] + [2] + [3].  The
+ * reference builds its Engine per Simulate call (Engine.cpp:19-73). */
+int nxm_get_create_timing(nxm_ctx *ctx, double ms[6], int32_t *autotune_cached);
+
+/* Layout of one system of the context: [0] cells per cell group (one block
+ * of the list-build and pair kernels per group), [1] atoms a staged
+ * neighbourhood can hold, [2..4] neighbour cells per axis, [5] list capacity
+ * per atom, [6] PME FFT launch shape in use (1 = line path, 2 = plane path),
+ * [7] 1 when the plane path transforms each x-plane in chunks of lines (the
+ * plane is larger than its shared-memory scratch), [8..10] FFT passes per
+ * axis.  No counterpart in the reference (its list and FFT have no layout). */
+int nxm_get_layout(nxm_ctx *ctx, int32_t system, int32_t out[11]);
+
+/* Radices of the FFT passes along one grid axis (0, 1, 2) of one system:
+ * returns the number of passes (at most cap radices written) or an error
+ * code.  Replaces FFTW's internal plan (NonbondedForce.cpp:264-290). */
+int nxm_get_fft_radices(nxm_ctx *ctx, int32_t system, int32_t axis, int32_t *radices, int32_t cap);
 
 /* Kernel launches one step issues (steady state, no list rebuild). */
 int nxm_launches_per_step(nxm_ctx *ctx, int32_t *launches, int32_t *rebuild_launches);
@@ -280,9 +327,16 @@ int nxm_dispatcher_simulate(nxm_dispatcher *d, const char *system_xml, const cha
  * allocating routine and copies nothing between host and device.
  * The first call on a device (the current one) looks up the array's address
  * (cudaGetSymbolAddress, which may load the module): make it before any
- * stream capture.  Every call on a device shares the array and finds the
- * previous call's contents; each call clears what must start at zero, but
- * calls whose work overlaps on the GPU race: serialise them. */
+ * stream capture.  That address is kept for the device's primary context: after
+ * cudaDeviceReset, unload and reload the library before calling again.  Every
+ * call on a device shares the array and finds the previous call's contents;
+ * each call clears what must start at zero, but calls whose work overlaps on
+ * the GPU race: serialise them.  A CUDA error already pending on the calling
+ * thread is returned as NXM_ERR_CUDA and left pending (not cleared).
+ * Results agree with the engine's PME step to force rel-RMS 1e-5 and energy
+ * 1e-5 relative, not bit for bit (charge grid rounded to the nearest 2^-32
+ * rather than truncated to 2^-31; influence function and moduli formed on
+ * the device; force converted from FP32 directly). */
 int nxm_pme_reciprocal_noalloc(const double *xyz, const double *charge, int32_t n_atoms,
                                const double box_lb[3], const double box_ub[3], const int32_t grid[3],
                                double alpha, double *force, double *energy, void *stream);

@@ -19,10 +19,14 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(HERE, "libnxm_cuda.so")
+# bench-only hardware probes (FP32 FMA peak, shared-memory atomics): a library
+# of their own beside bench.py, outside the engine and its C ABI
+PROBE_SRC = os.path.join(ROOT, "bench_probe.cu")
+PROBE_LIB = os.path.join(ROOT, "libnxm_probe.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["k_neighbor.cu", "k_pairs.cu", "k_bonded.cu", "k_nonbonded.cu", "k_fft.cu", "k_pme.cu",
                 "k_integrate.cu", "nxm_engine.cu", "nxm_abi.cpp", "nxm_dispatcher.cpp", "k_pme_noalloc.cu",
-                "nxm_report.cpp", "k_probe.cu"]
+                "nxm_report.cpp"]
 HOST_SOURCES = ["nxm_xml.cpp", "nxm_io.cpp"]
 
 
@@ -79,7 +83,30 @@ def build(verbose: bool = False) -> str:
     os.replace(tmp, LIB)
     if verbose:
         print("built", LIB)
+    build_probe(verbose)
     return LIB
+
+
+def build_probe(verbose: bool = False) -> str:
+    """Compile bench_probe.cu into libnxm_probe.so (bench.py's hardware probes)."""
+    os.makedirs(BUILD, exist_ok=True)
+    stamp = os.path.join(BUILD, "probe.stamp")
+    with open(PROBE_SRC, "rb") as f:
+        key = hashlib.sha256(f.read()).hexdigest()
+    if os.path.exists(PROBE_LIB) and os.path.exists(stamp) and open(stamp).read() == key:
+        return PROBE_LIB
+    tmp = PROBE_LIB + ".tmp"
+    cmd = [nvcc()] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
+                             PROBE_SRC, "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed for bench_probe.cu:\n" + r.stderr[-4000:])
+    os.replace(tmp, PROBE_LIB)
+    with open(stamp, "w") as f:
+        f.write(key)
+    if verbose:
+        print("built", PROBE_LIB)
+    return PROBE_LIB
 
 
 if __name__ == "__main__":

@@ -717,6 +717,7 @@ void fft_plan_build(FftPlan &p, int mixed) {
     long long room = (long long)budget - p.twcap - p.qcap;
     p.scr = (int)std::min<long long>(scr, room / 2);
     p.plane_ok = p.S > 0 && p.scr >= minscr;
+    p.plane_chunked = p.plane_ok && p.scr < scr;
     if (!p.plane_ok) p.plane = 0;
     p.smem_plane = ((size_t)p.twcap + p.qcap + 2 * (size_t)std::max(p.scr, 0)) * csz;
     // device buffers are kept across rebuilds of the same plan (the autotuner

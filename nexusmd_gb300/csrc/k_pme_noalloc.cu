@@ -18,7 +18,10 @@
 // Set-up: the first call on a device (the device current at the call) looks
 // up the array's device address with cudaGetSymbolAddress, once, and keeps
 // it; that lookup may load the module, so the first call on each device
-// should come before any stream capture.
+// should come before any stream capture.  The kept address belongs to the
+// device's primary context of that time: after cudaDeviceReset (which
+// destroys it) the library must be unloaded and loaded again before the
+// next call.
 //
 // Sharing: every call on a device uses the same array, which keeps the
 // previous call's contents.  Each call clears what must start at zero (the
@@ -395,7 +398,12 @@ extern "C" int nxm_pme_reciprocal_noalloc(const double *xyz, const double *charg
     v.total_grid = (long long)g.K[0] * g.K[1] * g.K[2];
     v.total_cgrid = (long long)g.K[0] * g.K[1] * g.Kh;
 
-    cudaGetLastError();  // clear a stale launch error from earlier work
+    // an error already pending on this thread belongs to the caller's earlier
+    // work: report it and leave it pending rather than clear it
+    cudaError_t pending = cudaPeekAtLastError();
+    if (pending != cudaSuccess)
+        return fail(NXM_ERR_CUDA, std::string(fn) + "a CUDA error was already pending: " +
+                                      cudaGetErrorString(pending));
     k_noalloc_setup<<<152, 256, 0, st>>>(scr, F, plan.nz, plan.ny, plan.nx);
     k_noalloc_eterm<<<(int)std::min<long long>((v.total_cgrid + 255) / 256, 1216), 256, 0, st>>>(scr, g);
     if (n_atoms > 0) k_noalloc_spread<<<(n_atoms + 127) / 128, 128, 0, st>>>(scr, g, xyz, charge, n_atoms);

@@ -249,6 +249,52 @@ int nxm_get_fft_plane_threads(nxm_ctx *ctx, int32_t *threads) {
     return NXM_OK;
 }
 
+int nxm_frames_init(nxm_ctx *ctx, int32_t depth) {
+    if (!ctx) return fail(NXM_ERR_INVALID, "null argument");
+    NXM_CALL(ctx->eng.frames_init(depth));
+}
+
+int nxm_step_async(nxm_ctx *ctx, int32_t nsteps, double dt) {
+    if (!ctx || nsteps <= 0) return fail(NXM_ERR_INVALID, "bad argument");
+    NXM_CALL(ctx->eng.step_async(nsteps, dt));
+}
+
+int nxm_frame_wait(nxm_ctx *ctx, const double **xyz, nxm_energies *energies, int32_t n_systems) {
+    if (!ctx || n_systems < 0 || (n_systems > 0 && !energies)) return fail(NXM_ERR_INVALID, "bad argument");
+    NXM_CALL(ctx->eng.frame_wait(xyz, energies, n_systems));
+}
+
+int nxm_get_create_timing(nxm_ctx *ctx, double ms[6], int32_t *autotune_cached) {
+    if (!ctx || !ms) return fail(NXM_ERR_INVALID, "null argument");
+    const double *c = ctx->eng.create_ms();
+    for (int k = 0; k < nxm::kCreatePhases; ++k) ms[k] = c[k];
+    if (autotune_cached) *autotune_cached = ctx->eng.autotune_cached();
+    return NXM_OK;
+}
+
+int nxm_get_pme_grids(nxm_ctx *ctx, int32_t system, double *charge, double *influence, double *potential) {
+    if (!ctx || system < 0 || system >= ctx->eng.n_systems()) return fail(NXM_ERR_INVALID, "bad argument");
+    NXM_CALL(ctx->eng.pme_grids(system, charge, influence, potential));
+}
+
+int nxm_get_layout(nxm_ctx *ctx, int32_t system, int32_t out[11]) {
+    if (!ctx || !out || system < 0 || system >= ctx->eng.n_systems()) return fail(NXM_ERR_INVALID, "bad argument");
+    int w[nxm::kLayoutWords];
+    ctx->eng.layout(system, w);
+    for (int k = 0; k < nxm::kLayoutWords; ++k) out[k] = w[k];
+    return NXM_OK;
+}
+
+int nxm_get_fft_radices(nxm_ctx *ctx, int32_t system, int32_t axis, int32_t *radices, int32_t cap) {
+    if (!ctx || system < 0 || system >= ctx->eng.n_systems() || axis < 0 || axis > 2 || cap < 0 ||
+        (cap > 0 && !radices))
+        return fail(NXM_ERR_INVALID, "bad argument");
+    int r[nxm::kMaxPasses];
+    int np = ctx->eng.fft_radices(system, axis, r, nxm::kMaxPasses);
+    for (int p = 0; p < np && p < cap; ++p) radices[p] = r[p];
+    return np;
+}
+
 int nxm_rebuild_count(nxm_ctx *ctx, int64_t *count) {
     if (!ctx || !count) return fail(NXM_ERR_INVALID, "null argument");
     std::string e = ctx->eng.sync();

@@ -8,12 +8,16 @@
 // (core/baseline/src/Engine.cpp:162-188) as a fixed sequence of kernel
 // launches on one stream, everything resident on the device.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <queue>
 #include <string>
 
 #include <thread>
+#include <tuple>
 
 #include "nxm_engine.h"
 
@@ -162,6 +166,7 @@ T *Engine::dalloc(size_t n) {
 
 Engine::~Engine() {
     if (st_) cudaStreamSynchronize(st_);
+    free_frames();
     free_graphs();
     for (void *p : allocs_) cudaFree(p);
     fft_plan_free(plan_);
@@ -179,8 +184,13 @@ std::string Engine::check(const char *what) {
     return "";
 }
 
+static double now_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
 std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_options &opt,
                          const double *positions) {
+    const double t_start = now_ms();
     if (systems.empty()) return "no systems";
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return "no CUDA device";
@@ -361,10 +371,13 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         hood_cap = std::max(hood_cap, hood);
         off += h.n;
     }
+    group_g_ = group_g;
     if (opt.max_neighbors > 0) stride = opt.max_neighbors;
     stride = (stride + 255) / 256 * 256;  // whole 256-entry chunks (transposed list layout)
 
     // ---- device memory
+    const double t_host = now_ms();
+    create_ms_[0] = t_host - t_start;
     cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking);
     // second stream and fork/join events: the PME branch of the step graph
     cudaStreamCreateWithFlags(&st_pme_, cudaStreamNonBlocking);
@@ -594,6 +607,8 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     }
 
     // ---- PME
+    const double t_dev = now_ms();
+    create_ms_[1] = t_dev - t_host;
     bool any_nb = false;
     for (auto &h : sysh_) any_nb |= (h.force_mask & NXM_FORCE_NONBONDED) != 0;
     v_.total_grid = roff;
@@ -685,6 +700,8 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         tune_[0] = plan_.plane ? 0 : plan_.zlines;
     }
     v_.pme_block = 128;
+    const double t_pme = now_ms();
+    create_ms_[2] = t_pme - t_dev;
     // systems without nonbonded forces: zero their charges in the PME and
     // pair paths by skipping them entirely (no list, no grid)
     v_.E = dalloc<long long>((size_t)S * E_SLOTS);
@@ -714,9 +731,33 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     cudaStreamSynchronize(st_);
     e = check("set-up");
     if (!e.empty()) return e;
-    if (opt.autotune && (v_.force_mask & NXM_FORCE_NONBONDED) && plan_.nz) return autotune();
-    return "";
+    // the allocations and uploads after the PME tables count with [1]
+    const double t_rest = now_ms();
+    create_ms_[1] += t_rest - t_pme;
+    if (opt.autotune && (v_.force_mask & NXM_FORCE_NONBONDED) && plan_.nz) e = autotune();
+    create_ms_[3] = now_ms() - t_rest;
+    create_ms_[5] = create_ms_[0] + create_ms_[1] + create_ms_[2] + create_ms_[3];
+    return e;
 }
+
+namespace {
+// Autotuned launch shapes per shape of batch within the process: the picks
+// change no result (see Engine::autotune), so a context with the same
+// device, precision, FFT path option, atom count and grids takes them
+// without timing the candidates again.
+struct TuneKey {
+    int device, mixed, fft_path, n;
+    std::vector<int> grids;
+    bool operator<(const TuneKey &o) const {
+        return std::tie(device, mixed, fft_path, n, grids) < std::tie(o.device, o.mixed, o.fft_path, o.n, o.grids);
+    }
+};
+struct TuneVal {
+    int zlines, cols, plane, plane_threads, pme_block;
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneVal> g_tune_cache;
+}  // namespace
 
 // Launch shapes that change no result, chosen by timing each candidate on
 // this context's own buffers (grid contents do not matter for the timing;
@@ -729,6 +770,27 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
 // summation order of the pair forces, and a choice that followed timing
 // noise would break run-to-run bit reproducibility.
 std::string Engine::autotune() {
+    TuneKey key{device_, mixed_, fft_path_, N_, {}};
+    for (auto &h : sysh_)
+        for (int d = 0; d < 3; ++d) key.grids.push_back(h.K[d]);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            const TuneVal &t = it->second;
+            plan_.zlines = t.zlines;
+            plan_.cols = t.cols;
+            fft_plan_build(plan_, mixed_);
+            plan_.plane = t.plane;
+            plan_.plane_threads = t.plane_threads;
+            v_.pme_block = t.pme_block;
+            tune_[0] = plan_.plane ? 0 : t.zlines;
+            tune_[1] = t.cols;
+            tune_[2] = t.pme_block;
+            autotune_cached_ = 1;
+            return check("autotune (cached)");
+        }
+    }
     cudaEvent_t a, b;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
@@ -806,6 +868,10 @@ std::string Engine::autotune() {
     tune_[0] = plan_.plane ? 0 : bz;
     tune_[1] = bc;
     tune_[2] = bt;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tune_cache[key] = TuneVal{bz, bc, bp, bpt, bt};
+    }
     return check("autotune");
 }
 
@@ -894,6 +960,13 @@ void Engine::free_graphs() {
 }
 
 std::string Engine::build_graph(double dt, int report) {
+    const double t0 = now_ms();
+    std::string r = build_graph_timed(dt, report);
+    create_ms_[4] += now_ms() - t0;
+    return r;
+}
+
+std::string Engine::build_graph_timed(double dt, int report) {
     StepGraph &G = graph_[report ? 1 : 0];
     if (G.exec) cudaGraphExecDestroy(G.exec);
     if (G.graph) cudaGraphDestroy(G.graph);
@@ -1012,6 +1085,73 @@ std::string Engine::enqueue_report(double *x, double *v, double *f, long long *E
     cudaMemcpyAsync(flags, v_.flags, sizeof(Flags), cudaMemcpyDeviceToHost, st_);
     cudaEventRecord(done, st_);
     return check("report copies");
+}
+
+void Engine::free_frames() {
+    for (Frame &f : ring_) {
+        if (f.done) cudaEventSynchronize(f.done);
+        if (f.x) cudaFreeHost(f.x);
+        if (f.E) cudaFreeHost(f.E);
+        if (f.flags) cudaFreeHost(f.flags);
+        if (f.done) cudaEventDestroy(f.done);
+    }
+    ring_.clear();
+    ring_next_ = ring_pending_ = 0;
+}
+
+std::string Engine::frames_init(int depth) {
+    if (depth < 1 || depth > 64) return "frame ring depth must be 1..64";
+    if (ring_pending_) return "frames still pending: wait for them first";
+    free_frames();
+    ring_.resize(depth);
+    for (Frame &f : ring_) {
+        if (cudaMallocHost(&f.x, sizeof(double) * 3 * (size_t)N_) != cudaSuccess ||
+            cudaMallocHost(&f.E, sizeof(long long) * energies_.size()) != cudaSuccess ||
+            cudaMallocHost(&f.flags, sizeof(Flags)) != cudaSuccess ||
+            cudaEventCreateWithFlags(&f.done, cudaEventDisableTiming) != cudaSuccess) {
+            free_frames();
+            return "device: pinned frame buffers could not be allocated";
+        }
+    }
+    return check("frames");
+}
+
+std::string Engine::step_async(int nsteps, double dt) {
+    if (ring_.empty()) {
+        std::string e = frames_init(2);
+        if (!e.empty()) return e;
+    }
+    Frame &f = ring_[ring_next_];
+    if (f.pending) return "frame ring full: wait for a frame before the next nxm_step_async";
+    for (int k = 0; k < nsteps; ++k) {
+        std::string e = one_step(dt, k == nsteps - 1);
+        if (!e.empty()) return e;
+    }
+    cudaMemcpyAsync(f.x, v_.snap_x, sizeof(double) * 3 * (size_t)N_, cudaMemcpyDeviceToHost, st_);
+    cudaMemcpyAsync(f.E, v_.E, sizeof(long long) * energies_.size(), cudaMemcpyDeviceToHost, st_);
+    cudaMemcpyAsync(f.flags, v_.flags, sizeof(Flags), cudaMemcpyDeviceToHost, st_);
+    cudaEventRecord(f.done, st_);
+    f.pending = true;
+    ring_next_ = (ring_next_ + 1) % (int)ring_.size();
+    ++ring_pending_;
+    return check("step_async");
+}
+
+std::string Engine::frame_wait(const double **xyz, nxm_energies *out, int n_out) {
+    if (!ring_pending_) return "no frame pending";
+    const int depth = (int)ring_.size();
+    Frame &f = ring_[(ring_next_ - ring_pending_ + depth) % depth];
+    cudaError_t ce = cudaEventSynchronize(f.done);
+    f.pending = false;
+    --ring_pending_;
+    if (ce != cudaSuccess) return std::string("device: ") + cudaGetErrorString(ce);
+    std::memcpy(h_flags_, f.flags, sizeof(Flags));
+    std::string e = flag_error(f.flags[0]);
+    if (!e.empty()) return e;
+    for (size_t k = 0; k < energies_.size(); ++k) energies_[k] = (double)f.E[k] * kEnergyUnscale;
+    for (int s = 0; s < n_out && s < (int)sysh_.size(); ++s) energies(s, &out[s]);
+    if (xyz) *xyz = f.x;
+    return "";
 }
 
 std::string Engine::step(int nsteps, double dt) {
@@ -1168,6 +1308,70 @@ void Engine::decode_energies(const double *e, const SysHost &H, nxm_energies *ou
     }
     out->potential = pe;
     out->reported_potential = reported;
+}
+
+std::string Engine::pme_grids(int s, double *charge, double *influence, double *potential) {
+    if (!v_.grid_acc || !(sysh_[s].force_mask & NXM_FORCE_NONBONDED)) return "no PME grids (nonbonded force off)";
+    cudaError_t ce = cudaStreamSynchronize(st_);
+    if (ce != cudaSuccess) return std::string("device: ") + cudaGetErrorString(ce);
+    const FftSysDev &F = plan_.hsys[s];
+    const size_t nr = (size_t)F.K[0] * F.K[1] * F.K[2], nc = (size_t)F.K[0] * F.K[1] * F.Kh;
+    auto fetch = [&](const void *base, size_t off, size_t n, size_t esz, std::vector<unsigned char> &h) {
+        h.resize(n * esz);
+        return cudaMemcpy(h.data(), static_cast<const unsigned char *>(base) + off * esz, n * esz,
+                          cudaMemcpyDeviceToHost);
+    };
+    std::vector<unsigned char> h;
+    if (charge) {
+        if (fetch(v_.grid_acc, F.roff, nr, 8, h) != cudaSuccess) return check("pme_grids");
+        for (size_t k = 0; k < nr; ++k) {
+            if (mixed_) {
+                long long w;
+                std::memcpy(&w, &h[8 * k], 8);
+                charge[k] = (double)w * kGridUnscale;
+            } else {
+                std::memcpy(&charge[k], &h[8 * k], 8);
+            }
+        }
+    }
+    const size_t fsz = mixed_ ? 4 : 8;
+    auto to_double = [&](double *out, size_t n) {
+        for (size_t k = 0; k < n; ++k) {
+            if (mixed_) {
+                float f;
+                std::memcpy(&f, &h[4 * k], 4);
+                out[k] = f;
+            } else {
+                std::memcpy(&out[k], &h[8 * k], 8);
+            }
+        }
+    };
+    if (influence) {
+        if (fetch(v_.eterm, F.coff, nc, fsz, h) != cudaSuccess) return check("pme_grids");
+        to_double(influence, nc);
+    }
+    if (potential) {
+        if (fetch(v_.grid_real, F.roff, nr, fsz, h) != cudaSuccess) return check("pme_grids");
+        to_double(potential, nr);
+    }
+    return check("pme_grids");
+}
+
+void Engine::layout(int s, int out[kLayoutWords]) const {
+    const SysDev &D = sysd_[s];
+    out[0] = group_g_[s];
+    out[1] = v_.hood_cap;
+    for (int d = 0; d < 3; ++d) out[2 + d] = D.nc[d];
+    out[5] = v_.stride;
+    out[6] = plan_.plane ? 2 : 1;
+    out[7] = plan_.plane_chunked;
+    for (int d = 0; d < 3; ++d) out[8 + d] = plan_.hsys[s].ax[d].np;
+}
+
+int Engine::fft_radices(int s, int d, int *out, int cap) const {
+    const FftPasses &P = plan_.hsys[s].ax[d];
+    for (int p = 0; p < P.np && p < cap; ++p) out[p] = P.R[p];
+    return P.np;
 }
 
 std::string Engine::pairs(int s, std::vector<int> &out) {

@@ -12,6 +12,8 @@
 namespace nxm {
 
 constexpr int kProfilePhases = 8;
+constexpr int kLayoutWords = 11;
+constexpr int kCreatePhases = 6;
 
 struct HostSystem {
     int n = 0;
@@ -72,6 +74,16 @@ public:
     // words) and the device flags (8 ints) into caller-owned pinned host
     // buffers, then records `done`.  Nothing waits.
     std::string enqueue_report(double *x, double *v, double *f, long long *E, int *flags, cudaEvent_t done);
+    // Pipelined stepping: a ring of pinned host slots owned by the engine,
+    // each holding one report step's positions (original order, 3N
+    // doubles), energy words and flags, filled by copies on the engine
+    // stream.  step_async enqueues nsteps steps (the last a report step) and
+    // the copies into the next free slot and returns; frame_wait waits for
+    // the oldest filled slot and hands out its positions (valid until that
+    // slot is filled again) and the energies of the first n_out systems.
+    std::string frames_init(int depth);
+    std::string step_async(int nsteps, double dt);
+    std::string frame_wait(const double **xyz, nxm_energies *out, int n_out);
     int energy_words() const { return (int)energies_.size(); }
     // Energies of system s from accumulators copied by enqueue_report.
     void energies_from(const long long *raw, int s, nxm_energies *out) const;
@@ -82,6 +94,11 @@ public:
     std::string get_state(double *x, double *v);
     void energies(int sys, nxm_energies *out) const;
     std::string pairs(int sys, std::vector<int> &out);
+    // System s's PME grids of the last evaluation, as doubles: the charge
+    // grid the spread summed (K0 K1 K2), the influence function on the half
+    // spectrum (K0 K1 (K2/2+1)) and the real grid after the convolution and
+    // inverse transform (K0 K1 K2); any pointer may be null.
+    std::string pme_grids(int s, double *charge, double *influence, double *potential);
     std::string time_steps(int nsteps, double dt, double *ms);
     std::string profile(int nsteps, double dt, double *ms);
     int n_total() const { return N_; }
@@ -92,6 +109,21 @@ public:
     const int *tuning() const { return tune_; }
     // threads per plane-path FFT block, 0 on the line path
     int fft_plane_threads() const { return plan_.plane ? plan_.plane_threads : 0; }
+    // System s's layout: [0] cells per group, [1] neighbourhood capacity
+    // (atoms), [2..4] cells per axis, [5] list stride, [6] FFT path in use
+    // (1 lines, 2 planes), [7] 1 when the plane path works through a plane in
+    // chunks of lines, [8..10] FFT passes per axis.
+    void layout(int s, int out[kLayoutWords]) const;
+    // Radices of system s's FFT passes along axis d (count returned, at most
+    // cap written).
+    int fft_radices(int s, int d, int *out, int cap) const;
+    // Host wall milliseconds of context creation: [0] host set-up (box,
+    // constants, exclusions), [1] device allocation and uploads, [2] PME
+    // tables and FFT plan, [3] autotuning (0 when skipped or cached),
+    // [4] step-graph builds so far, [5] creation total ([0]..[3]).
+    const double *create_ms() const { return create_ms_; }
+    // 1 when the launch shapes came from an earlier context of the same shapes
+    int autotune_cached() const { return autotune_cached_; }
     // neighbour-list rebuilds since creation, as of the last finished call
     long long rebuild_count() const { return h_flags_ ? reinterpret_cast<const Flags *>(h_flags_)->nrebuild : 0; }
 
@@ -113,6 +145,7 @@ private:
     int tune_[3] = {0, 8, 128};
     std::string autotune();
     std::string build_graph(double dt, int report);
+    std::string build_graph_timed(double dt, int report);
     void free_graphs();
     std::string one_step(double dt, int report);
     std::string check(const char *what);
@@ -132,6 +165,19 @@ private:
     int mixed_ = 1;
     int interval_ = 1;
     int fft_path_ = 0;  // nxm_options::fft_path
+    std::vector<int> group_g_;  // cells per group, per system
+    double create_ms_[kCreatePhases] = {};
+    struct Frame {
+        double *x = nullptr;      // pinned, 3N
+        long long *E = nullptr;   // pinned, energy words
+        int *flags = nullptr;     // pinned, Flags
+        cudaEvent_t done = nullptr;
+        bool pending = false;
+    };
+    std::vector<Frame> ring_;
+    int ring_next_ = 0, ring_pending_ = 0;
+    void free_frames();
+    int autotune_cached_ = 0;
     bool force_rebuild_ = true;
     int since_rebuild_ = 0;
     std::vector<void *> allocs_;

@@ -57,6 +57,7 @@ struct FftPlan {
     FftWork *pwork = nullptr;
     int npl = 0;
     int plane = 0, plane_ok = 0;
+    int plane_chunked = 0;  // a plane is larger than the scratch: the plane path works in chunks of lines
     int plane_threads = 512;
     int twcap = 0, qcap = 0, scr = 0;   // shared-memory regions, complex words
     size_t smem_plane = 0;

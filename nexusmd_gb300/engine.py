@@ -93,6 +93,14 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.nxm_rebuild_count.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
     L.nxm_get_tuning.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
     L.nxm_get_fft_plane_threads.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
+    L.nxm_frames_init.argtypes = [C.c_void_p, C.c_int32]
+    L.nxm_step_async.argtypes = [C.c_void_p, C.c_int32, C.c_double]
+    L.nxm_frame_wait.argtypes = [C.c_void_p, C.POINTER(C.POINTER(C.c_double)), C.POINTER(Energies), C.c_int32]
+    L.nxm_get_pme_grids.argtypes = [C.c_void_p, C.c_int32, dp, dp, dp]
+    L.nxm_get_create_timing.argtypes = [C.c_void_p, dp, C.POINTER(C.c_int32)]
+    L.nxm_get_layout.argtypes = [C.c_void_p, C.c_int32, np.ctypeslib.ndpointer(np.int32)]
+    L.nxm_get_fft_radices.argtypes = [C.c_void_p, C.c_int32, C.c_int32, np.ctypeslib.ndpointer(np.int32),
+                                      C.c_int32]
     L.nxm_n_atoms.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
     L.nxm_save_state.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_int64, C.c_double]
     _lib = L
@@ -101,6 +109,22 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
 
 class NxmError(RuntimeError):
     pass
+
+
+def pair_digest(pairs, n_atoms):
+    """Order-independent digest of a pair set: (count, sum over pairs of a
+    64-bit mix of the key i * n + j, modulo 2^64).  Two sets with equal
+    digests are equal except with probability ~2^-64; used where the sets
+    (10^8 pairs) are too large to sort and compare in reasonable time."""
+    p = np.asarray(pairs).reshape(-1, 2)
+    with np.errstate(over="ignore"):
+        k = p[:, 0].astype(np.uint64) * np.uint64(n_atoms) + p[:, 1].astype(np.uint64)
+        # splitmix64 finaliser
+        k = k + np.uint64(0x9E3779B97F4A7C15)
+        k = (k ^ (k >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        k = (k ^ (k >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        k = k ^ (k >> np.uint64(31))
+        return int(len(p)), int(k.sum(dtype=np.uint64))
 
 
 def _check(rc, what=""):
@@ -252,8 +276,9 @@ class Engine:
         _check(self._L.nxm_get_alpha(self._h, int(system), C.byref(a)), "get_alpha")
         return a.value
 
-    def pairs(self, system=0):
-        """Neighbour pair set within the cutoff, sorted rows (i, j), i > j."""
+    def pairs(self, system=0, sort=True):
+        """Neighbour pair set within the cutoff, rows (i, j), i > j; sorted
+        by (i, j) unless ``sort`` is False."""
         n = self._L.nxm_get_pairs(self._h, int(system), np.zeros(2, np.int32), 0)
         if n < 0:
             _check(int(n), "get_pairs")
@@ -262,7 +287,66 @@ class Engine:
         if n2 < 0:
             _check(int(n2), "get_pairs")
         p = out[:2 * n].reshape(-1, 2)
-        return p[np.lexsort((p[:, 1], p[:, 0]))]
+        return p[np.lexsort((p[:, 1], p[:, 0]))] if sort else p
+
+    def step_async(self, nsteps, dt):
+        """Enqueue nsteps steps and the copy of the last one's frame into the
+        pinned ring; returns without waiting."""
+        _check(self._L.nxm_step_async(self._h, int(nsteps), float(dt)), "step_async")
+
+    def frame_wait(self, copy=True):
+        """The oldest pending frame: (positions [n][3], energies of system 0).
+        With copy=False the positions are a view of the pinned ring slot,
+        valid until that slot is filled again."""
+        p = C.POINTER(C.c_double)()
+        e = Energies()
+        _check(self._L.nxm_frame_wait(self._h, C.byref(p), C.byref(e), 1), "frame_wait")
+        x = np.ctypeslib.as_array(p, shape=(self.n_atoms, 3))
+        return (x.copy() if copy else x), e.as_dict()
+
+    def pme_grids(self, system=0):
+        """(charge grid [K0,K1,K2], influence function [K0,K1,K2//2+1], real
+        grid after convolution and inverse transform [K0,K1,K2]) of the last
+        force evaluation."""
+        K = self.grid(system)
+        q = np.zeros(K)
+        e = np.zeros((K[0], K[1], K[2] // 2 + 1))
+        r = np.zeros(K)
+        _check(self._L.nxm_get_pme_grids(self._h, int(system), q, e, r), "get_pme_grids")
+        return q, e, r
+
+    CREATE_PHASES = ("host_setup", "device_alloc_upload", "pme_tables_fft_plan", "autotune", "graph_builds",
+                     "create_total")
+
+    def create_timing(self):
+        """Host milliseconds of context creation by phase, and whether the
+        autotuned launch shapes came from an earlier context of the same shapes."""
+        ms = np.zeros(len(self.CREATE_PHASES))
+        cached = C.c_int32()
+        _check(self._L.nxm_get_create_timing(self._h, ms, C.byref(cached)), "get_create_timing")
+        d = dict(zip(self.CREATE_PHASES, ms.tolist()))
+        d["autotune_cached"] = bool(cached.value)
+        return d
+
+    LAYOUT = ("cells_per_group", "hood_capacity", "cells_x", "cells_y", "cells_z", "list_stride",
+              "fft_path", "fft_plane_chunked", "fft_passes_x", "fft_passes_y", "fft_passes_z")
+
+    def layout(self, system=0):
+        """Cell groups, neighbourhood capacity, cells, list stride and FFT
+        plan of one system (``fft_path`` 1 = line path, 2 = plane path) plus
+        ``fft_radices``: the radix of each FFT pass per axis."""
+        out = np.zeros(len(self.LAYOUT), np.int32)
+        _check(self._L.nxm_get_layout(self._h, int(system), out), "get_layout")
+        d = dict(zip(self.LAYOUT, (int(x) for x in out)))
+        r = []
+        for ax in range(3):
+            buf = np.zeros(16, np.int32)
+            k = self._L.nxm_get_fft_radices(self._h, int(system), ax, buf, len(buf))
+            if k < 0:
+                _check(int(k), "get_fft_radices")
+            r.append(tuple(int(x) for x in buf[:k]))
+        d["fft_radices"] = tuple(r)
+        return d
 
     PHASES = ("rebuild", "bonded", "pairs", "exclusions", "spread", "fft", "gather", "integrate")
 

@@ -14,7 +14,20 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_TREE = os.environ.get("NXM_REFERENCE_TREE", "/root/reference")
+# The reference's source tree (its NexusMD/ directory's parent), named by the
+# build recipe through NXM_REFERENCE_TREE; without it only a reference library
+# built earlier (_ref/libnxm_ref.so) can be used.
+REF_TREE = os.environ.get("NXM_REFERENCE_TREE") or None
+REF_LIB = os.path.join(HERE, "_ref", "libnxm_ref.so")
+
+
+def reference_tree_present() -> bool:
+    return bool(REF_TREE) and os.path.isdir(os.path.join(REF_TREE, "NexusMD", "core"))
+
+
+def reference_available() -> bool:
+    """The reference library exists or can be built from its tree."""
+    return reference_tree_present() or os.path.exists(REF_LIB)
 
 _dp = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
@@ -23,11 +36,13 @@ _ip = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 def build(ref: bool | None = None) -> None:
     """Compile liboracle.so (and the reference library when its tree exists)."""
     targets = ["oracle"]
-    if ref is None:
-        ref = os.path.isdir(os.path.join(REF_TREE, "NexusMD", "core"))
+    if ref is None or (ref and not reference_tree_present()):
+        # without the tree a reference library built earlier is used as it is
+        ref = reference_tree_present()
     if ref:
         targets.append("ref")
-    subprocess.run(["make", "-s", "-j8", "-C", HERE, "REF=" + REF_TREE] + targets, check=True)
+    cmd = ["make", "-s", "-j8", "-C", HERE] + (["REF=" + REF_TREE] if ref else []) + targets
+    subprocess.run(cmd, check=True)
 
 
 class Box(C.Structure):
@@ -196,7 +211,10 @@ class Oracle:
 
     def neighbor_pairs(self, pos, box, eoff, elst, cutoff):
         p = _c(pos, np.float64)
-        cap = 300 * len(p) + 1024
+        # first capacity from the density: pairs ~ (2/3) pi rc^3 n^2 / V, plus a margin
+        vol = float(np.prod(np.asarray(list(box.size))))
+        est = 2.0 / 3.0 * np.pi * cutoff ** 3 * len(p) * len(p) / vol if vol > 0 else 300.0 * len(p)
+        cap = int(1.25 * est) + 1024
         while True:
             out = np.zeros(2 * cap, np.int32)
             np_ = self.lib.nxo_neighbor_pairs(len(p), p, C.byref(box), _c(eoff, np.int32),

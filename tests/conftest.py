@@ -23,8 +23,8 @@ def oracle():
 def reference():
     """The reference compiled from its own sources (skips where its tree is absent)."""
     from oracle import nxo
-    if not os.path.isdir(os.path.join(nxo.REF_TREE, "NexusMD", "core")):
-        pytest.skip("reference source tree not present on this machine")
+    if not nxo.reference_available():
+        pytest.skip("reference library not built and NXM_REFERENCE_TREE not set")
     nxo.build(ref=True)
     return nxo.Reference()
 

@@ -6,8 +6,12 @@ within the cutoff, so the engine's nonbonded force (nxm_compute_forces +
 nxm_get_forces) is the reciprocal-space force alone and nxm_get_energies'
 `recip` is the reciprocal energy.  Both entry points are called through the
 C ABI; the new one gets device buffers made by torch (the test allocates,
-the entry point does not).  Two calls in a row with different grids check
-that no state left in the shared array leaks into the next call.
+the entry point does not).  Two calls in a row with different grids, then
+the first grid again, check that no state left in the shared array leaks
+into the next call: the repeated call must give the first call's numbers
+bit for bit (the fixed-point charge grid makes each call deterministic).
+The same calls are also checked against the FP64 oracle's reciprocal force
+and energy (the reference's PME restated, NonbondedForce.cpp:51-461).
 
 This file sorts last so that it also runs after every other test; it passes
 alone in a fresh process as well.
@@ -81,7 +85,7 @@ def _rel_rms(a, b):
     return float(np.sqrt(np.mean((a - b) ** 2)) / np.sqrt(np.mean(b ** 2)))
 
 
-def test_noalloc_pme_matches_engine_on_consecutive_calls():
+def test_noalloc_pme_matches_engine_on_consecutive_calls(oracle):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
@@ -90,19 +94,47 @@ def test_noalloc_pme_matches_engine_on_consecutive_calls():
     dev = torch.device("cuda", 0)
     xyz_d = torch.tensor(s.pos, dtype=torch.float64, device=dev).contiguous()
     q_d = torch.tensor(s.charge, dtype=torch.float64, device=dev).contiguous()
+    box = oracle.box_explicit([0.0, 0.0, 0.0], list(s.box))
     results = []
-    for grid in ((40, 36, 30), (32, 32, 32)):
+    for grid in ((40, 36, 30), (32, 32, 32), (40, 36, 30)):
         F_ref, E_ref, alpha = _engine_reciprocal(s, grid)
         rc, F, E = _noalloc(f, xyz_d, q_d, s.box, grid, alpha, torch)
         assert rc == 0, L.nxm_last_error().decode()
         err = _rel_rms(F, F_ref)
-        print("grid", grid, "force rel-RMS", err, "energy", E, "engine", E_ref)
+        E_o, F_o = oracle.pme(s.pos, s.charge, box, alpha, np.array(grid, np.int32))
+        err_o = _rel_rms(F, F_o)
+        print("grid", grid, "force rel-RMS vs engine", err, "vs oracle", err_o, "energy", E, "engine", E_ref,
+              "oracle", E_o)
         assert np.isfinite(F).all()
         assert err <= MIXED_FORCE_TOL, (grid, err)
         assert abs(E - E_ref) <= MIXED_ENERGY_TOL * abs(E_ref), (grid, E, E_ref)
+        assert err_o <= MIXED_FORCE_TOL, (grid, err_o)
+        assert abs(E - E_o) <= MIXED_ENERGY_TOL * abs(E_o), (grid, E, E_o)
         results.append((F, E))
-    # the second grid differs, so its result must too (nothing stale reused)
+    # the second grid differs, so its result must too; the third call repeats
+    # the first grid after the second left its contents in the shared array,
+    # and must reproduce the first call exactly
     assert results[0][1] != results[1][1]
+    assert np.array_equal(results[2][0], results[0][0])
+    assert results[2][1] == results[0][1]
+
+
+def test_noalloc_pme_no_atoms_after_charged_call():
+    """A call with no atoms, right after a charged one, finds nothing stale:
+    its energy is exactly zero."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    s = _lattice_system(n=50)
+    L, f = _bind()
+    dev = torch.device("cuda", 0)
+    xyz_d = torch.tensor(s.pos, dtype=torch.float64, device=dev).contiguous()
+    q_d = torch.tensor(s.charge, dtype=torch.float64, device=dev).contiguous()
+    rc, _, E = _noalloc(f, xyz_d, q_d, s.box, (32, 32, 32), 5.0, torch)
+    assert rc == 0 and E != 0.0
+    rc, _, E0 = _noalloc(f, xyz_d[:0], q_d[:0], s.box, (32, 32, 32), 5.0, torch)
+    assert rc == 0, L.nxm_last_error().decode()
+    assert E0 == 0.0
 
 
 def test_noalloc_pme_rejects_grid_above_limit():
