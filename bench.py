@@ -432,6 +432,8 @@ def other_workload(cfg, steps, warmup, device, check=True, fp64_steps=0):
         r = {"value": sig(n * k_steps / (ms * 1e-3)), "unit": "atom-steps/s", "ms_per_step": sig(ms / k_steps),
              "ns_per_day": sig((1.0 / (ms / k_steps * 1e-3)) * DT_PS * 1e-3 * 86400.0), "steps": k_steps,
              "list_rebuilds": eng.rebuilds() - rb0}
+        if prec == 1:
+            r["phase_ms"] = {k: sig(v, 3) for k, v in eng.profile(20, DT_PS).items()}
         if check:
             eng.set_positions(pos0)
             # pair sets of 10^8 pairs (config 5) by digest, the rest sorted
@@ -507,6 +509,28 @@ def e2e_run(s, v0, kw, steps):
     create = eng.create_timing()
     eng.close()
     return dt, create
+
+
+def fft_paths(cfg, device):
+    """Per-step FFT + convolution time (phase profile, CUDA events) of the
+    line path and of the plane path on configuration cfg's system."""
+    from nexusmd_gb300.engine import Engine
+    s = make_system(cfg)
+    out = {}
+    for path, name in ((1, "lines"), (2, "planes")):
+        eng = Engine(s, precision=1, skin=0.1, rebuild_interval=10, box="explicit", device=device,
+                     exceptions=True, fft_path=path)
+        lay = eng.layout()
+        if lay["fft_path"] != path:
+            out[name] = None
+        else:
+            eng.step(3, DT_PS)
+            out[name] = {"fft_ms": sig(eng.profile(20, DT_PS)["fft"], 3),
+                         "plane_chunked": bool(lay["fft_plane_chunked"]) if path == 2 else None}
+        eng.close()
+    out["grid"] = list(s.grid)
+    out["radices"] = [list(r) for r in lay["fft_radices"]]
+    return out
 
 
 def workload_config(name, s):
@@ -627,6 +651,10 @@ def native(args):
                            "shared_atomics_per_clk_sm": {"u64": sig(u64 or 0.0), "u32": sig(u32 or 0.0)}}
         out["roofline_hbm"] = dict(hbm, peak_source="MEASURED_PEAKS.json hbm_gbs (%s)" % src)
         out["phase_ms"] = {k: sig(v, 3) for k, v in ph.items()}
+        # a step that computes energies and the snapshot (every step of a
+        # loop that reports each step, as the end-to-end loop does)
+        out["report_step_ms"] = sig(eng.time_report_steps(max(20, min(200, args.steps)), DT_PS) /
+                                    max(20, min(200, args.steps)))
         # the same end-to-end measurement over 1,000 steps
         t_long, _ = e2e_run(s, v0, kw, 1000)
         out["e2e"]["value_1000_steps"] = sig(s.n * 1000 / t_long)
@@ -660,6 +688,7 @@ def native(args):
                 for k in ("c2", "c4", "c5"):
                     out["pair_set"][k] = ow[k]["mixed"]["pair_set"]
                 out["pair_set"]["c2_fp64"] = ow["c2"]["fp64"]["pair_set"]
+            out["fft_paths"] = {"c3": fft_paths(3, local), "c5": fft_paths(5, local)}
             out["simulate_reporting"] = [reporting(1, 400, 1, local), reporting(3, 50, 1, local),
                                          reporting(3, 100, 10, local)]
         if not args.no_cpu:

@@ -192,6 +192,10 @@ int64_t nxm_get_pairs(nxm_ctx *ctx, int32_t system, int32_t *pairs, int64_t cap)
  * context's stream, after the call's launches); milliseconds. */
 int nxm_time_steps(nxm_ctx *ctx, int32_t nsteps, double dt, double *ms);
 
+/* The same for nsteps steps that each compute the energies and the x/v/F
+ * snapshot, as the steps of a loop that reports every step do. */
+int nxm_time_report_steps(nxm_ctx *ctx, int32_t nsteps, double dt, double *ms);
+
 /* Average device milliseconds per step of each phase over nsteps steps
  * (CUDA events between phases on the context's stream; no energies):
  * [0] list rebuild decision + rebuild, [1] bonded, [2] real-space pairs,
@@ -231,9 +235,10 @@ int nxm_get_pme_grids(nxm_ctx *ctx, int32_t system, double *charge, double *infl
  * and FFT plan, [3] autotuning of launch shapes (about 0 when autotune is
  * off or an earlier context of the same shapes in this process was tuned:
  * *autotune_cached = 1), [4] step-graph builds so far (the first steps
- * build them), [5] the creation total [0] + [1] + [2] + [3].  The
+ * build them), [5] the creation total [0] + [1] + [2] + [3]; and, within
+ * [1], [6] device allocation with zeroing and [7] host-to-device copies.  The
  * reference builds its Engine per Simulate call (Engine.cpp:19-73). */
-int nxm_get_create_timing(nxm_ctx *ctx, double ms[6], int32_t *autotune_cached);
+int nxm_get_create_timing(nxm_ctx *ctx, double ms[8], int32_t *autotune_cached);
 
 /* Layout of one system of the context: [0] cells per cell group (one block
  * of the list-build and pair kernels per group), [1] atoms a staged

@@ -5,9 +5,12 @@
 // (core/baseline/src/Forces/HarmonicBondForce.cpp:20-58,
 //  HarmonicAngleForce.cpp:19-63, PeriodicTorsionForce.cpp:41-149).
 // Displacements are always formed from the FP64 positions with the
-// reference's single-shift minimum image; in mixed mode they are then
-// rounded to FP32 (the stiff bond terms cannot afford FP32 positions) and the
-// rest of the term is FP32 with int64 fixed-point force accumulation.
+// reference's single-shift minimum image.  In mixed mode they are formed
+// exactly in 2^-40 nm fixed point from the bits of the FP64 positions with
+// integer instructions (fix40: this GPU's FP64 pipe is narrow) and rounded
+// once to FP32 (the stiff bond terms cannot afford FP32 positions); the rest
+// of the term is FP32 with FP32 parameters and int64 fixed-point force
+// accumulation.
 #include "nxm_pairterms.cuh"
 #include "nxm_view.h"
 
@@ -39,15 +42,30 @@ __device__ __forceinline__ V3<R> scale(const V3<R> &a, R s) {
 template <typename R>
 __device__ __forceinline__ V3<R> disp(const DevView &v, const SysDev &S, int a, int b) {
     if (sizeof(R) == 4) {
-        // FP64 difference, shift decided in FP32 (min_image_f)
-        return mk<R>((R)min_image_f(v.x[a] - v.x[b], S.L[0], S.halfLf[0]),
-                     (R)min_image_f(v.y[a] - v.y[b], S.L[1], S.halfLf[1]),
-                     (R)min_image_f(v.z[a] - v.z[b], S.L[2], S.halfLf[2]));
+        // exact fixed-point difference, integer minimum image, one rounding
+        return mk<R>((R)min_image40(fix40(v.x[a]) - fix40(v.x[b]), S.L40[0], S.halfL40[0]),
+                     (R)min_image40(fix40(v.y[a]) - fix40(v.y[b]), S.L40[1], S.halfL40[1]),
+                     (R)min_image40(fix40(v.z[a]) - fix40(v.z[b]), S.L40[2], S.halfL40[2]));
     }
     double dx = min_image(v.x[a] - v.x[b], S.L[0], S.halfL[0]);
     double dy = min_image(v.y[a] - v.y[b], S.L[1], S.halfL[1]);
     double dz = min_image(v.z[a] - v.z[b], S.L[2], S.halfL[2]);
     return mk<R>((R)dx, (R)dy, (R)dz);
+}
+
+// A term's two parameters in the arithmetic's precision (FP32 copies made
+// at set-up in mixed mode).
+template <typename R>
+__device__ __forceinline__ void term_prm(const double2 *p64, const float2 *p32, int k, R &a, R &b) {
+    if (sizeof(R) == 4) {
+        const float2 p = p32[k];
+        a = (R)p.x;
+        b = (R)p.y;
+    } else {
+        const double2 p = p64[k];
+        a = (R)p.x;
+        b = (R)p.y;
+    }
 }
 
 template <typename Acc, typename R>
@@ -98,7 +116,7 @@ __global__ void __launch_bounds__(256) k_bonded(DevView v, int energy, int pairs
     const int nbt = v.nb + v.na + v.nt;
     const int nx = pairs ? v.nex : 0, nc = pairs ? v.nxc : 0;
     int total = nbt;
-    double e = 0.0;
+    R e = 0;  // this thread's term energy (mixed: FP32, summed as fixed point)
     int term = -1, sys = 0;
     if (t >= nbt && t < nbt + nx) {
         term = E_EXCL;
@@ -112,14 +130,15 @@ __global__ void __launch_bounds__(256) k_bonded(DevView v, int energy, int pairs
             // HarmonicBondForce.cpp:20-58
             term = E_BOND;
             int2 b = v.bond_slot[t];
-            double2 p = v.bond_prm[t];
+            R p0, p1;  // d, k
+            term_prm<R>(v.bond_prm, v.bond_prmf, t, p0, p1);
             sys = v.sys_of[b.x];
             const SysDev &S = v.sys[sys];
             V3<R> d = disp<R>(v, S, b.y, b.x);
             R r = r_sqrt<R>(dot(d, d));
-            R dI = r - (R)p.x;
-            e = (double)((R)0.5 * (R)p.y * dI * dI);
-            R dEdR = (R)p.y * dI;
+            R dI = r - p0;
+            if (energy) e = (R)0.5 * p1 * dI * dI;
+            R dEdR = p1 * dI;
             d = r > (R)0 ? scale(d, dEdR / r) : mk<R>(0, 0, 0);
             add_force<Acc>(v, b.x, d);
             add_force<Acc>(v, b.y, scale(d, (R)-1));
@@ -128,7 +147,8 @@ __global__ void __launch_bounds__(256) k_bonded(DevView v, int energy, int pairs
             term = E_ANGLE;
             int k = t - v.nb;
             int4 a = v.angle_slot[k];
-            double2 p = v.angle_prm[k];
+            R p0, p1;  // a, k
+            term_prm<R>(v.angle_prm, v.angle_prmf, k, p0, p1);
             sys = v.sys_of[a.x];
             const SysDev &S = v.sys[sys];
             V3<R> v0 = disp<R>(v, S, a.y, a.x);
@@ -139,9 +159,9 @@ __global__ void __launch_bounds__(256) k_bonded(DevView v, int energy, int pairs
             R c = dot(v0, v1) / (r21 * r23);
             c = c < (R)-1 ? (R)-1 : (c > (R)1 ? (R)1 : c);
             R theta = r_acos<R>(c);
-            R dI = theta - (R)p.x;
-            e = (double)((R)0.5 * (R)p.y * dI * dI);
-            R dEdA = (R)p.y * dI;
+            R dI = theta - p0;
+            if (energy) e = (R)0.5 * p1 * dI * dI;
+            R dEdA = p1 * dI;
             R rp = r_sqrt<R>(dot(cp, cp));
             rp = rp < (R)1.0e-06 ? (R)1.0e-06 : rp;
             V3<R> f1 = scale(cross(v0, cp), dEdA / (q21 * rp));
@@ -155,7 +175,8 @@ __global__ void __launch_bounds__(256) k_bonded(DevView v, int energy, int pairs
             term = E_TORSION;
             int k = t - v.nb - v.na;
             int4 a = v.tors_slot[k];
-            double2 p = v.tors_prm[k];
+            R p0, p1;  // k, phase
+            term_prm<R>(v.tors_prm, v.tors_prmf, k, p0, p1);
             int per = v.tors_per[k];
             sys = v.sys_of[a.x];
             const SysDev &S = v.sys[sys];
@@ -175,11 +196,11 @@ __global__ void __launch_bounds__(256) k_bonded(DevView v, int energy, int pairs
                 ang = r_acos<R>(cosang);
             }
             ang = dot(v0, cp1) >= (R)0 ? ang : -ang;
-            R dA = (R)per * ang - (R)p.y;
+            R dA = (R)per * ang - p1;
             R sn, cs;
             r_sincos<R>(dA, &sn, &cs);
-            e = (double)((R)p.x * ((R)1 + cs));
-            R dEdPhi = -(R)p.x * (R)per * sn;
+            if (energy) e = p0 * ((R)1 + cs);
+            R dEdPhi = -p0 * (R)per * sn;
             R nc1 = dot(cp0, cp0), nbc2 = dot(v1, v1), nc2 = dot(cp1, cp1);
             R nbc = r_sqrt<R>(nbc2);
             R dp = (R)1 / nbc2;
@@ -197,10 +218,10 @@ __global__ void __launch_bounds__(256) k_bonded(DevView v, int energy, int pairs
     }
     if (energy) {
         // each energy term reduced separately (all lanes participate)
-        for (int k = E_BOND; k <= E_TORSION; ++k) energy_add(v.E, sys, k, term == k ? e : 0.0);
+        for (int k = E_BOND; k <= E_TORSION; ++k) energy_add_t(v.E, sys, k, term == k ? e : (R)0);
         if (pairs) {
-            energy_add(v.E, sys, E_EXCL, term == E_EXCL ? e : 0.0);
-            energy_add(v.E, sys, E_EXCEPT, term == E_EXCEPT ? e : 0.0);
+            energy_add_t(v.E, sys, E_EXCL, term == E_EXCL ? e : (R)0);
+            energy_add_t(v.E, sys, E_EXCEPT, term == E_EXCEPT ? e : (R)0);
         }
     }
 }

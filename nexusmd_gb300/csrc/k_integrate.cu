@@ -17,7 +17,8 @@ __global__ void __launch_bounds__(256) k_integrate(DevView v, double dt, int rep
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     bool live = s < v.N;
     int sys = live ? v.sys_of[s] : 0;
-    double ke = 0.0;
+    double ke = 0.0;   // FP64 engine
+    float kef = 0.0f;  // mixed engine (summed as fixed point)
     if (live) {
         const SysDev &S = v.sys[sys];
         Acc *ax = static_cast<Acc *>(v.fx) + s;
@@ -46,7 +47,7 @@ __global__ void __launch_bounds__(256) k_integrate(DevView v, double dt, int rep
                                      __uint2float_rn((unsigned)(wc & 0xffffff)) * 2.3283064365386963e-10f;  // 2^-32
                     vh[c] = fmaf(fc, kf, (float)u[c]);
                 }
-                ke = (double)(0.5f * (float)m * fmaf(vh[0], vh[0], fmaf(vh[1], vh[1], vh[2] * vh[2])));
+                kef = 0.5f * (float)m * fmaf(vh[0], vh[0], fmaf(vh[1], vh[1], vh[2] * vh[2]));
             } else {
                 double vh[3] = {u[0], u[1], u[2]};
                 if (m > 0) {
@@ -68,16 +69,18 @@ __global__ void __launch_bounds__(256) k_integrate(DevView v, double dt, int rep
         if (im != 0.0 && v.mixed) {
             // fixed-point forces: v += (invm dt 2^-32) * word, one multiply-add per
             // component on the FP64 pipe (the order of the two scalings differs
-            // from the FP64 engine's only in the last bit)
+            // from the FP64 engine's only in the last bit).  The wrap test
+            // compares order-preserving integer keys of the doubles (the same
+            // outcome as the FP64 comparison, off the narrow FP64 pipe); the
+            // shift itself is FP64 and is taken only when an atom crosses.
             const double c0 = im * (dt * kForceUnscale);
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 u[c] = fma(c0, (double)w[c], u[c]);
                 double q = fma(u[c], dt, p[c]);
-                if (q < S.lb[c])
-                    q += S.L[c];
-                else if (q > S.ub[c])
-                    q -= S.L[c];
+                const long long kq = dkey(q);
+                const int out = kq < S.lbkey[c] ? 1 : (kq > S.ubkey[c] ? -1 : 0);
+                if (__builtin_expect(out != 0, 0)) q += out > 0 ? S.L[c] : -S.L[c];
                 p[c] = q;
             }
             v.x[s] = p[0];
@@ -105,15 +108,17 @@ __global__ void __launch_bounds__(256) k_integrate(DevView v, double dt, int rep
             v.vz[s] = u[2];
         }
         if (v.mixed) {
-            // One FP64 subtraction per component serves both the FP32 cell
+            // One exact fixed-point displacement per component (integer
+            // instructions on the positions' bits) serves both the FP32 cell
             // offset (offset at the last rebuild + displacement since) and
             // the skin check; shifts and squares in FP32, which keeps this
             // kernel off the slow FP64 pipe except for the update itself.
             float4 r = v.oref[s];
             float d[3], d2 = 0.0f;
+            const long long *xref40 = reinterpret_cast<const long long *>(v.xref);
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                d[c] = min_image_f(p[c] - v.xref[(size_t)c * v.N + s], S.L[c], S.halfLf[c]);
+                d[c] = min_image40(fix40(p[c]) - xref40[(size_t)c * v.N + s], S.L40[c], S.halfL40[c]);
                 d2 = fmaf(d[c], d[c], d2);
             }
             v.pf[s] = make_float4(r.x + d[0], r.y + d[1], r.z + d[2], r.w);
@@ -133,7 +138,12 @@ __global__ void __launch_bounds__(256) k_integrate(DevView v, double dt, int rep
             if (!(isfinite(F(0)) && isfinite(F(1)) && isfinite(F(2)))) atomicOr(&v.flags->error, ERR_NONFINITE);
         }
     }
-    if (report) energy_add(v.E, sys, E_KIN, ke);
+    if (report) {
+        if (v.mixed)
+            energy_add_f(v.E, sys, E_KIN, kef);
+        else
+            energy_add(v.E, sys, E_KIN, ke);
+    }
 }
 
 // Copy positions, velocities and (optionally) the accumulated forces to the

@@ -213,9 +213,18 @@ __global__ void k_derive(DevView v, int gated) {
         v.qs[s] = qs;
         v.ljd[s] = make_double2(sg, ep);
     }
-    v.xref[s] = x;
-    v.xref[v.N + s] = y;
-    v.xref[2 * v.N + s] = z;
+    if (v.mixed) {
+        // the mixed integrator's skin test and cell offsets take
+        // displacements from these in fixed point (fix40)
+        long long *x40 = reinterpret_cast<long long *>(v.xref);
+        x40[s] = fix40(x);
+        x40[v.N + s] = fix40(y);
+        x40[2 * v.N + s] = fix40(z);
+    } else {
+        v.xref[s] = x;
+        v.xref[v.N + s] = y;
+        v.xref[2 * v.N + s] = z;
+    }
 }
 
 __global__ void k_remap(DevView v) {

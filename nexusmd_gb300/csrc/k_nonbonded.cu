@@ -9,19 +9,19 @@ namespace nxm {
 template <bool MIXED>
 __global__ void __launch_bounds__(256) k_exclusions(DevView v, int energy) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
-    double e = 0.0;
+    TermE<MIXED> e = 0;
     int sys = 0;
     if (t < v.nex) e = exclusion_pair<MIXED>(v, t, sys);
-    if (energy) energy_add(v.E, sys, E_EXCL, e);
+    if (energy) energy_add_t(v.E, sys, E_EXCL, e);
 }
 
 template <bool MIXED>
 __global__ void __launch_bounds__(256) k_exceptions(DevView v, int energy) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
-    double e = 0.0;
+    TermE<MIXED> e = 0;
     int sys = 0;
     if (t < v.nxc) e = exception_pair<MIXED>(v, t, sys);
-    if (energy) energy_add(v.E, sys, E_EXCEPT, e);
+    if (energy) energy_add_t(v.E, sys, E_EXCEPT, e);
 }
 void launch_exceptions(const DevView &v, int energy, cudaStream_t st) {
     if (v.nxc == 0) return;

@@ -547,8 +547,8 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_pairs_mixed(DevView v) {
             ev = ecv.y;
         }
         // each pair sits in both partners' lists
-        energy_add(v.E, G.sys, E_COUL, 0.5 * (double)ec);
-        energy_add(v.E, G.sys, E_VDW, 0.5 * (double)ev);
+        energy_add_f(v.E, G.sys, E_COUL, 0.5f * ec);
+        energy_add_f(v.E, G.sys, E_VDW, 0.5f * ev);
     }
 }
 

@@ -231,6 +231,11 @@ int nxm_time_steps(nxm_ctx *ctx, int32_t nsteps, double dt, double *ms) {
     NXM_CALL(ctx->eng.time_steps(nsteps, dt, ms));
 }
 
+int nxm_time_report_steps(nxm_ctx *ctx, int32_t nsteps, double dt, double *ms) {
+    if (!ctx || !ms || nsteps <= 0) return fail(NXM_ERR_INVALID, "bad argument");
+    NXM_CALL(ctx->eng.time_steps(nsteps, dt, ms, 1));
+}
+
 int nxm_profile_phases(nxm_ctx *ctx, int32_t nsteps, double dt, double *ms, int32_t cap) {
     if (!ctx || !ms || nsteps <= 0 || cap < nxm::kProfilePhases) return fail(NXM_ERR_INVALID, "bad argument");
     NXM_CALL(ctx->eng.profile(nsteps, dt, ms));
@@ -264,7 +269,7 @@ int nxm_frame_wait(nxm_ctx *ctx, const double **xyz, nxm_energies *energies, int
     NXM_CALL(ctx->eng.frame_wait(xyz, energies, n_systems));
 }
 
-int nxm_get_create_timing(nxm_ctx *ctx, double ms[6], int32_t *autotune_cached) {
+int nxm_get_create_timing(nxm_ctx *ctx, double ms[8], int32_t *autotune_cached) {
     if (!ctx || !ms) return fail(NXM_ERR_INVALID, "null argument");
     const double *c = ctx->eng.create_ms();
     for (int k = 0; k < nxm::kCreatePhases; ++k) ms[k] = c[k];

@@ -8,6 +8,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 namespace nxm {
 
@@ -84,6 +85,12 @@ struct SysDev {
     // along axis d (integer part, fraction); kl = K / L
     int cg_off[3];
     float kl[3];
+    // box edge and half edge as multiples of 2^-40 nm (fix40), for the
+    // minimum image of fixed-point displacements
+    long long L40[3], halfL40[3];
+    // order-preserving integer keys (dkey) of the box corners, for the
+    // update's wrap test without FP64 comparisons
+    long long lbkey[3], ubkey[3];
 };
 
 // Flags word layout in device memory.
@@ -98,6 +105,57 @@ struct Flags {
 };
 
 // ----------------------------------------------------------------- helpers
+
+// Positions in fixed point.  This GPU issues FP64 instructions (arithmetic,
+// comparisons and conversions alike) at a small fraction of its FP32 and
+// integer rates, yet a displacement between two nearby atoms needs FP64
+// precision only until it is rounded to FP32.  fix40(x) = x * 2^40 rounded
+// to the nearest integer (half away from zero), formed from the bits of the
+// double with integer instructions only; exact to 2^-41 nm for |x| < 2^22 nm.
+// The difference of two such values is the displacement to 2^-40 nm, and
+// its minimum image is an integer compare-and-add.
+__host__ __device__ __forceinline__ long long fix40(double x) {
+    long long b;
+#ifdef __CUDA_ARCH__
+    b = __double_as_longlong(x);
+#else
+    memcpy(&b, &x, sizeof b);
+#endif
+    const int e = (int)((b >> 52) & 0x7ff);
+    const long long m = (b & 0xfffffffffffffLL) | 0x10000000000000LL;
+    const int sh = 1035 - e;  // x * 2^40 = m * 2^(e - 1035)
+    long long r = sh <= 0 ? (m << (-sh < 9 ? -sh : 9)) : (sh < 62 ? ((m >> (sh - 1)) + 1) >> 1 : 0);
+    r = e == 0 ? 0 : r;
+    return b < 0 ? -r : r;
+}
+
+// d * 2^-40 rounded once to FP32 (|d| < 2^45): d = hi 2^21 + lo with
+// |hi| < 2^24 and 0 <= lo < 2^21, both exact in FP32, so the fused
+// multiply-add rounds the exact value.
+__device__ __forceinline__ float fix40_to_float(long long d) {
+    const float hi = (float)(int)(d >> 21);
+    const float lo = (float)(int)(d & 0x1fffff);
+    return fmaf(hi, 1.9073486328125e-06f /* 2^-19 */, lo * 9.094947017729282e-13f /* 2^-40 */);
+}
+
+// The reference's single-shift minimum image (PeriodicBoundaryCondition.cpp
+// :93-104) on a fixed-point displacement, rounded to FP32.
+__device__ __forceinline__ float min_image40(long long d, long long L40, long long halfL40) {
+    d = d > halfL40 ? d - L40 : (d < -halfL40 ? d + L40 : d);
+    return fix40_to_float(d);
+}
+
+// An integer key with the order of the doubles it comes from (non-NaN):
+// dkey(a) < dkey(b) exactly when a < b, -0 and +0 equal.
+__host__ __device__ __forceinline__ long long dkey(double x) {
+    long long b;
+#ifdef __CUDA_ARCH__
+    b = __double_as_longlong(x);
+#else
+    memcpy(&b, &x, sizeof b);
+#endif
+    return b < 0 ? (long long)((unsigned long long)0x8000000000000000ULL - (unsigned long long)b) : b;
+}
 
 __device__ __forceinline__ void atomic_add_fixed(long long *a, double v, double scale) {
     atomicAdd(reinterpret_cast<unsigned long long *>(a),
@@ -170,6 +228,37 @@ __device__ __forceinline__ void energy_add(long long *E, int sys, int term, doub
         atomic_add_fixed(&E[sys * E_SLOTS + term], v, kEnergyScale);
     }
 }
+
+// v * 2^28 (the energy unit) rounded to an integer with FP32 and integer
+// instructions only: v = h + l with h = rint(v) and l = v - h, both exact in
+// FP32, so h 2^28 is exact and l 2^28 rounds once (|v| < 2^31).
+__device__ __forceinline__ long long energy_fixed(float v) {
+    const float h = rintf(v);
+    const float l = v - h;
+    return ((long long)__float2int_rn(h) << 28) + (long long)__float2int_rn(l * 268435456.0f);
+}
+
+// Energy accumulation of the FP32 kernels: each lane's FP32 partial is
+// converted to fixed point (energy_fixed) and the warp sums the integers --
+// no FP64 instruction, order-free, one atomic per warp when every lane is in
+// one system (per lane otherwise).
+__device__ __forceinline__ void energy_add_f(long long *E, int sys, int term, float v) {
+    const unsigned full = 0xffffffffu;
+    long long w = energy_fixed(v);
+    const int s0 = __shfl_sync(full, sys, 0);
+    if (__all_sync(full, sys == s0)) {
+        for (int o = 16; o; o >>= 1) w += __shfl_xor_sync(full, w, o);
+        if ((threadIdx.x & 31) == 0 && w != 0)
+            atomicAdd(reinterpret_cast<unsigned long long *>(&E[s0 * E_SLOTS + term]), static_cast<unsigned long long>(w));
+    } else if (w != 0) {
+        atomicAdd(reinterpret_cast<unsigned long long *>(&E[sys * E_SLOTS + term]), static_cast<unsigned long long>(w));
+    }
+}
+
+// The energy sum of either arithmetic: FP32 partials as fixed point, FP64
+// partials by the FP64 warp sum.
+__device__ __forceinline__ void energy_add_t(long long *E, int sys, int term, float v) { energy_add_f(E, sys, term, v); }
+__device__ __forceinline__ void energy_add_t(long long *E, int sys, int term, double v) { energy_add(E, sys, term, v); }
 
 // Adds one fixed-point energy per lane (units of 1 / kEnergyScale) of a
 // warp whose lanes all belong to system `sys`: integer sums, so the total does

@@ -119,49 +119,177 @@ static void bspline_moduli(int K, std::vector<double> &mod) {
 }
 
 // Exclusions.cpp:7-44 with bondCutoff = depth: every atom reachable through
-// 1..depth bonds.
-static std::string exclusions(const HostSystem &s, std::vector<std::vector<int>> &ex) {
-    int n = s.n;
-    std::vector<std::vector<int>> adj(n);
-    for (size_t b = 0; b < s.bonds.size() / 2; ++b) {
+// 1..depth bonds, united with the exception partners (pairs `exc`, which are
+// excluded from the Ewald direct sum too).  Appends one sorted row per atom
+// of the system to the batch CSR (eoff, elst), indices shifted by `off`, and
+// the pairs with j > i to ex_pairs.  Flat arrays only: the bonds' adjacency
+// by a counting sort, one breadth-first search per atom into a shared
+// buffer, then a merge with the atom's sorted exception partners.
+static std::string exclusion_rows(const HostSystem &s, int off, std::vector<int> &eoff, std::vector<int> &elst,
+                                  std::vector<int2> &ex_pairs) {
+    const int n = s.n;
+    const size_t nbond = s.bonds.size() / 2;
+    std::vector<int> aoff(n + 1, 0), adj(2 * nbond);
+    for (size_t b = 0; b < nbond; ++b) {
         int i = s.bonds[2 * b], j = s.bonds[2 * b + 1];
         if (i < 0 || j < 0 || i >= n || j >= n) return "createExclusions: Illegal particle index in list of bonds";
-        adj[i].push_back(j);
-        adj[j].push_back(i);
+        ++aoff[i + 1];
+        ++aoff[j + 1];
     }
-    ex.assign(n, {});
-    if (s.excl_depth < 1) return "";
-    std::vector<int> dist(n, -1), queue;
-    for (int i = 0; i < n; ++i) {
-        queue.clear();
-        queue.push_back(i);
-        dist[i] = 0;
-        for (size_t h = 0; h < queue.size(); ++h) {
-            int u = queue[h];
-            if (dist[u] == s.excl_depth) continue;
-            for (int w : adj[u])
-                if (dist[w] < 0) {
-                    dist[w] = dist[u] + 1;
-                    queue.push_back(w);
-                    ex[i].push_back(w);
-                }
+    for (int i = 0; i < n; ++i) aoff[i + 1] += aoff[i];
+    {
+        std::vector<int> fill(aoff.begin(), aoff.end() - 1);
+        for (size_t b = 0; b < nbond; ++b) {
+            int i = s.bonds[2 * b], j = s.bonds[2 * b + 1];
+            adj[fill[i]++] = j;
+            adj[fill[j]++] = i;
         }
-        for (int u : queue) dist[u] = -1;
-        std::sort(ex[i].begin(), ex[i].end());
+    }
+    // exception partners, sorted per atom
+    const size_t nexc = s.exc.size() / 2;
+    std::vector<int> xoff(n + 1, 0), xadj(2 * nexc);
+    for (size_t k = 0; k < nexc; ++k) {
+        ++xoff[s.exc[2 * k] + 1];
+        ++xoff[s.exc[2 * k + 1] + 1];
+    }
+    for (int i = 0; i < n; ++i) xoff[i + 1] += xoff[i];
+    {
+        std::vector<int> fill(xoff.begin(), xoff.end() - 1);
+        for (size_t k = 0; k < nexc; ++k) {
+            int a = s.exc[2 * k], b = s.exc[2 * k + 1];
+            xadj[fill[a]++] = b;
+            xadj[fill[b]++] = a;
+        }
+        for (int i = 0; i < n; ++i) std::sort(xadj.begin() + xoff[i], xadj.begin() + xoff[i + 1]);
+    }
+    std::vector<int> dist(n, -1), queue, row;
+    queue.reserve(64);
+    row.reserve(64);
+    for (int i = 0; i < n; ++i) {
+        row.clear();
+        if (s.excl_depth >= 1) {
+            queue.clear();
+            queue.push_back(i);
+            dist[i] = 0;
+            for (size_t h = 0; h < queue.size(); ++h) {
+                int u = queue[h];
+                if (dist[u] == s.excl_depth) continue;
+                for (int k = aoff[u]; k < aoff[u + 1]; ++k) {
+                    int w = adj[k];
+                    if (dist[w] < 0) {
+                        dist[w] = dist[u] + 1;
+                        queue.push_back(w);
+                        row.push_back(w);
+                    }
+                }
+            }
+            for (int u : queue) dist[u] = -1;
+            std::sort(row.begin(), row.end());
+        }
+        // sorted union with the exception partners
+        const size_t base = elst.size();
+        size_t p = 0;
+        int q = xoff[i];
+        while (p < row.size() || q < xoff[i + 1]) {
+            int v;
+            if (q >= xoff[i + 1] || (p < row.size() && row[p] < xadj[q]))
+                v = row[p++];
+            else if (p >= row.size() || xadj[q] < row[p])
+                v = xadj[q++];
+            else {
+                v = row[p++];
+                ++q;
+            }
+            if (elst.size() > base && elst.back() == off + v) continue;  // repeated exception pair
+            elst.push_back(off + v);
+            if (v > i) ex_pairs.push_back(make_int2(off + i, off + v));
+        }
+        eoff.push_back((int)elst.size());
     }
     return "";
 }
 
+// reciprocalConvolutionAndEnergy's eterm (NonbondedForce.cpp:323-388) on one
+// system's half spectrum, one thread per element, in FP64 with the host's
+// order of operations written out (round-to-nearest multiplies and adds, no
+// fused multiply-adds); the element (0, 0, 0) is zero.  mod: the three axes'
+// B-spline moduli, concatenated.
+template <typename T>
+__global__ void k_influence(T *eterm, const double *mod, int K0, int K1, int K2, double r0, double r1, double r2,
+                            double factor, double boxfactor) {
+    const int Kh = K2 / 2 + 1;
+    const long long n = (long long)K0 * K1 * Kh;
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= n) return;
+    const int kz = (int)(idx % Kh);
+    const long long t = idx / Kh;
+    const int ky = (int)(t % K1), kx = (int)(t / K1);
+    if (idx == 0) {
+        eterm[0] = (T)0;
+        return;
+    }
+    const double mx = kx < (K0 + 1) / 2 ? kx : kx - K0;
+    const double my = ky < (K1 + 1) / 2 ? ky : ky - K1;
+    const double mz = kz < (K2 + 1) / 2 ? kz : kz - K2;
+    const double mhx = __dmul_rn(mx, r0), mhy = __dmul_rn(my, r1), mhz = __dmul_rn(mz, r2);
+    const double m2 = __dadd_rn(__dadd_rn(__dmul_rn(mhx, mhx), __dmul_rn(mhy, mhy)), __dmul_rn(mhz, mhz));
+    const double bx = __dmul_rn(boxfactor, mod[kx]), by = mod[K0 + ky], bz = mod[K0 + K1 + kz];
+    const double denom = __dmul_rn(__dmul_rn(__dmul_rn(m2, bx), by), bz);
+    eterm[idx] = (T)__ddiv_rn(__dmul_rn(kOne4PiEps0, exp(__dmul_rn(-factor, m2))), denom);
+}
+
+static void launch_influence(void *eterm, int mixed, long long coff, const double *mod, const int K[3],
+                             const double L[3], double alpha, cudaStream_t st) {
+    const long long n = (long long)K[0] * K[1] * (K[2] / 2 + 1);
+    const int nb = (int)((n + 255) / 256);
+    const double r0 = 1 / L[0], r1 = 1 / L[1], r2 = 1 / L[2];
+    const double factor = kPi * kPi / (alpha * alpha);
+    const double boxfactor = kPi * L[0] * L[1] * L[2];
+    if (mixed)
+        k_influence<float><<<nb, 256, 0, st>>>(static_cast<float *>(eterm) + coff, mod, K[0], K[1], K[2], r0, r1, r2,
+                                               factor, boxfactor);
+    else
+        k_influence<double><<<nb, 256, 0, st>>>(static_cast<double *>(eterm) + coff, mod, K[0], K[1], K[2], r0, r1,
+                                                r2, factor, boxfactor);
+}
+
 // ------------------------------------------------------------ engine
+
+static double now_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// Zeroed device arrays.  Arrays up to a quarter of a chunk come out of 32 MB
+// chunks, 256-byte aligned (one cudaMalloc and one memset per chunk);
+// larger ones get an allocation of their own.  Freed with the engine.
+constexpr size_t kArenaChunk = 32u << 20;
 
 template <typename T>
 T *Engine::dalloc(size_t n) {
-    void *p = nullptr;
     if (n == 0) n = 1;
-    if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) return nullptr;
-    cudaMemset(p, 0, n * sizeof(T));
-    allocs_.push_back(p);
-    return static_cast<T *>(p);
+    const size_t bytes = (n * sizeof(T) + 255) & ~(size_t)255;
+    auto fresh = [&](size_t b) -> char * {
+        const double t0 = now_ms();
+        void *p = nullptr;
+        if (cudaMalloc(&p, b) != cudaSuccess) {
+            alloc_failed_ = true;
+            return nullptr;
+        }
+        cudaMemset(p, 0, b);
+        allocs_.push_back(p);
+        create_ms_[6] += now_ms() - t0;
+        return static_cast<char *>(p);
+    };
+    if (bytes > kArenaChunk / 4) return reinterpret_cast<T *>(fresh(bytes));
+    if (arena_left_ < bytes) {
+        arena_ptr_ = fresh(kArenaChunk);
+        arena_left_ = arena_ptr_ ? kArenaChunk : 0;
+        if (!arena_ptr_) return nullptr;
+    }
+    T *r = reinterpret_cast<T *>(arena_ptr_);
+    arena_ptr_ += bytes;
+    arena_left_ -= bytes;
+    return r;
 }
 
 Engine::~Engine() {
@@ -170,8 +298,7 @@ Engine::~Engine() {
     free_graphs();
     for (void *p : allocs_) cudaFree(p);
     fft_plan_free(plan_);
-    if (h_E_) cudaFreeHost(h_E_);
-    if (h_flags_) cudaFreeHost(h_flags_);
+    if (h_E_) cudaFreeHost(h_E_);  // h_flags_ lies in the same block
     if (ev_fork_) cudaEventDestroy(ev_fork_);
     if (ev_join_) cudaEventDestroy(ev_join_);
     if (st_pme_) cudaStreamDestroy(st_pme_);
@@ -182,10 +309,6 @@ std::string Engine::check(const char *what) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return std::string(what) + ": " + cudaGetErrorString(e);
     return "";
-}
-
-static double now_ms() {
-    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
 std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_options &opt,
@@ -214,7 +337,8 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     sysh_.assign(S, SysHost{});
     plan_.S = S;
     plan_.hsys.assign(S, FftSysDev{});
-    std::vector<std::vector<int>> excl_all(N_);
+    // exclusion sets as batch CSR (original indices), filled per system
+    std::vector<int> eoff(1, 0), elst;
     std::vector<int2> ex_pairs;
     std::vector<int2> xc_pairs;      // exception pairs, batch-global original indices
     std::vector<double4> xc_prm;
@@ -288,6 +412,12 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         D.a04 = (float)(0.4 * H.alpha);
         D.k2a = (float)(2.0 * H.alpha / kSqrtPi);
         for (int d = 0; d < 3; ++d) D.csf[d] = (float)D.cs[d];
+        for (int d = 0; d < 3; ++d) {
+            D.L40[d] = fix40(H.L[d]);
+            D.halfL40[d] = fix40(0.5 * H.L[d]);
+            D.lbkey[d] = dkey(H.lb[d]);
+            D.ubkey[d] = dkey(H.ub[d]);
+        }
         D.rlist2f = (float)D.rlist2;
         D.sw_distf = (float)h.sw_dist;
         D.cutofff = (float)h.cutoff;
@@ -317,34 +447,20 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         roff += (long long)H.K[0] * H.K[1] * H.K[2];
         coff += (long long)H.K[0] * H.K[1] * D.Kh;
 
-        // exclusions (batch-global original indices)
-        std::vector<std::vector<int>> ex;
-        std::string err = exclusions(h, ex);
-        if (!err.empty()) return err;
-        // exception pairs are excluded from the Ewald direct sum too
+        // exclusions (batch-global original indices), united with the
+        // exception pairs, which are excluded from the Ewald direct sum too
         if (h.exc.size() != 2 * (h.exc_prm.size() / 3)) return "exception arrays disagree in length";
         for (size_t k = 0; k < h.exc.size() / 2; ++k) {
             int a = h.exc[2 * k], b = h.exc[2 * k + 1];
             if (a < 0 || b < 0 || a >= h.n || b >= h.n || a == b) return "exception: illegal particle index";
-            ex[a].push_back(b);
-            ex[b].push_back(a);
             if (h.force_mask & NXM_FORCE_NONBONDED) {
                 xc_pairs.push_back(make_int2(off + a, off + b));
                 const double *p = &h.exc_prm[3 * k];
                 xc_prm.push_back(make_double4(kOne4PiEps0 * p[0], p[1], 4.0 * p[2], 0.0));
             }
         }
-        if (!h.exc.empty())
-            for (auto &l : ex) {
-                std::sort(l.begin(), l.end());
-                l.erase(std::unique(l.begin(), l.end()), l.end());
-            }
-        for (int i = 0; i < h.n; ++i) {
-            for (int j : ex[i]) {
-                excl_all[off + i].push_back(off + j);
-                if (j > i) ex_pairs.push_back(make_int2(off + i, off + j));
-            }
-        }
+        std::string err = exclusion_rows(h, off, eoff, elst, ex_pairs);
+        if (!err.empty()) return err;
         // list capacity from the density
         double vol = H.L[0] * H.L[1] * H.L[2];
         double expect = 4.0 / 3.0 * kPi * H.rlist * H.rlist * H.rlist * h.n / vol;
@@ -471,7 +587,11 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
             }
         }
     }
-    auto up = [&](void *dst, const void *src, size_t bytes) { cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice); };
+    auto up = [&](void *dst, const void *src, size_t bytes) {
+        const double t0 = now_ms();
+        cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+        create_ms_[7] += now_ms() - t0;
+    };
     up(v_.sys_of, sys_of.data(), sizeof(int) * N_);
     up(v_.orig, iota.data(), sizeof(int) * N_);
     up(v_.slot_of, iota.data(), sizeof(int) * N_);
@@ -516,12 +636,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         up(v_.cgrid, cg.data(), sizeof(float2) * cg.size());
     }
 
-    // exclusion CSR (batch-global original indices)
-    std::vector<int> eoff(N_ + 1, 0), elst;
-    for (int i = 0; i < N_; ++i) {
-        eoff[i + 1] = eoff[i] + (int)excl_all[i].size();
-        elst.insert(elst.end(), excl_all[i].begin(), excl_all[i].end());
-    }
+    // exclusion CSR (batch-global original indices), built per system above
     v_.excl_off = dalloc<int>(N_ + 1);
     v_.excl_lst = dalloc<int>(elst.size());
     up(v_.excl_off, eoff.data(), sizeof(int) * (N_ + 1));
@@ -586,6 +701,22 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         up(v_.tors_prm, tp.data(), sizeof(double2) * v_.nt);
         up(v_.tors_per, tper.data(), sizeof(int) * v_.nt);
     }
+    if (mixed_) {
+        // the FP32 engine's parameters rounded once here rather than in
+        // every evaluation (the same values: the kernels round the same doubles)
+        auto f2 = [](const std::vector<double2> &a) {
+            std::vector<float2> o(a.size());
+            for (size_t k = 0; k < a.size(); ++k) o[k] = make_float2((float)a[k].x, (float)a[k].y);
+            return o;
+        };
+        std::vector<float2> bf = f2(bp), af = f2(ap), tf = f2(tp);
+        v_.bond_prmf = dalloc<float2>(v_.nb);
+        v_.angle_prmf = dalloc<float2>(v_.na);
+        v_.tors_prmf = dalloc<float2>(v_.nt);
+        if (v_.nb) up(v_.bond_prmf, bf.data(), sizeof(float2) * v_.nb);
+        if (v_.na) up(v_.angle_prmf, af.data(), sizeof(float2) * v_.na);
+        if (v_.nt) up(v_.tors_prmf, tf.data(), sizeof(float2) * v_.nt);
+    }
     // exclusion correction pairs: only for systems with nonbonded enabled
     {
         std::vector<int2> keep;
@@ -604,6 +735,13 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     if (v_.nxc) {
         up(v_.xc_orig, xc_pairs.data(), sizeof(int2) * v_.nxc);
         up(v_.xc_prm, xc_prm.data(), sizeof(double4) * v_.nxc);
+    }
+    if (mixed_) {
+        std::vector<float4> xf(xc_prm.size());
+        for (size_t k = 0; k < xc_prm.size(); ++k)
+            xf[k] = make_float4((float)xc_prm[k].x, (float)xc_prm[k].y, (float)xc_prm[k].z, 0.f);
+        v_.xc_prmf = dalloc<float4>(v_.nxc);
+        if (v_.nxc) up(v_.xc_prmf, xf.data(), sizeof(float4) * v_.nxc);
     }
 
     // ---- PME
@@ -637,59 +775,33 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         } else {
             up(v_.twiddle, tw.data(), sizeof(double) * tw.size());
         }
-        // influence function on the half spectrum, NonbondedForce.cpp:323-388
-        std::vector<double> et((size_t)coff, 0.0);
+        // influence function on the half spectrum, NonbondedForce.cpp:323-388:
+        // B-spline moduli on the host (once per distinct grid length), the
+        // elements on the device (k_influence)
+        std::vector<double> mods;
+        std::vector<size_t> mod_off(S);
+        {
+            std::map<int, std::vector<double>> by_len;
+            for (int s = 0; s < S; ++s) {
+                mod_off[s] = mods.size();
+                for (int d = 0; d < 3; ++d) {
+                    const int K = sysh_[s].K[d];
+                    auto it = by_len.find(K);
+                    if (it == by_len.end()) {
+                        std::vector<double> m;
+                        bspline_moduli(K, m);
+                        it = by_len.emplace(K, std::move(m)).first;
+                    }
+                    mods.insert(mods.end(), it->second.begin(), it->second.end());
+                }
+            }
+        }
+        double *dmod = dalloc<double>(mods.size());
+        up(dmod, mods.data(), sizeof(double) * mods.size());
         for (int s = 0; s < S; ++s) {
             const SysHost &H = sysh_[s];
             if (!(H.force_mask & NXM_FORCE_NONBONDED)) continue;
-            std::vector<double> mod[3];
-            for (int d = 0; d < 3; ++d) bspline_moduli(H.K[d], mod[d]);
-            double recip[3] = {1 / H.L[0], 1 / H.L[1], 1 / H.L[2]};
-            double one_4pi_eps = kOne4PiEps0 / 1.0;
-            double factor = kPi * kPi / (H.alpha * H.alpha);
-            double boxfactor = kPi * H.L[0] * H.L[1] * H.L[2];
-            int K0 = H.K[0], K1 = H.K[1], K2 = H.K[2], Kh = K2 / 2 + 1;
-            int maxkx = (K0 + 1) / 2, maxky = (K1 + 1) / 2, maxkz = (K2 + 1) / 2;
-            double *e = et.data() + plan_.hsys[s].coff;
-            // one x-plane per task over the host's threads: every element is
-            // computed on its own, so the values do not depend on the split
-            auto plane = [&](int kx) {
-                double mx = (kx < maxkx) ? kx : (kx - K0);
-                double mhx = mx * recip[0];
-                double bx = boxfactor * mod[0][kx];
-                for (int ky = 0; ky < K1; ++ky) {
-                    double my = (ky < maxky) ? ky : (ky - K1);
-                    double mhy = my * recip[1];
-                    double by = mod[1][ky];
-                    for (int kz = 0; kz < Kh; ++kz) {
-                        size_t idx = ((size_t)kx * K1 + ky) * Kh + kz;
-                        if (kx == 0 && ky == 0 && kz == 0) {
-                            e[idx] = 0.0;
-                            continue;
-                        }
-                        double mz = (kz < maxkz) ? kz : (kz - K2);
-                        double mhz = mz * recip[2];
-                        double m2 = mhx * mhx + mhy * mhy + mhz * mhz;
-                        double bz = mod[2][kz];
-                        double denom = m2 * bx * by * bz;
-                        e[idx] = one_4pi_eps * std::exp(-factor * m2) / denom;
-                    }
-                }
-            };
-            const int nth = std::max(1, std::min<int>(K0, (int)std::thread::hardware_concurrency()));
-            std::vector<std::thread> pool;
-            for (int t = 1; t < nth; ++t)
-                pool.emplace_back([&, t] {
-                    for (int kx = t; kx < K0; kx += nth) plane(kx);
-                });
-            for (int kx = 0; kx < K0; kx += nth) plane(kx);
-            for (auto &th : pool) th.join();
-        }
-        if (mixed_) {
-            std::vector<float> ef(et.begin(), et.end());
-            up(v_.eterm, ef.data(), sizeof(float) * ef.size());
-        } else {
-            up(v_.eterm, et.data(), sizeof(double) * et.size());
+            launch_influence(v_.eterm, mixed_, plan_.hsys[s].coff, dmod + mod_off[s], H.K, H.L, H.alpha, st_);
         }
         v_.pme_idx = dalloc<int4>(N_);
         v_.pme_frac = mixed_ ? (void *)dalloc<float4>(N_) : (void *)dalloc<double2>(2 * (size_t)N_);
@@ -719,11 +831,16 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     for (auto &h : sysh_) v_.force_mask |= h.force_mask;
     v_.any_switch = 0;
     for (auto &d : sysd_) v_.any_switch |= d.use_switch ? 1 : 0;
-    cudaMallocHost(&h_E_, sizeof(long long) * S * E_SLOTS);
-    cudaMallocHost(&h_flags_, sizeof(Flags));
+    // the energy words and the flags in one pinned block (pinning is slow per call)
+    {
+        void *hp = nullptr;
+        const size_t be = (sizeof(long long) * S * E_SLOTS + 255) & ~(size_t)255;
+        if (cudaMallocHost(&hp, be + sizeof(Flags)) != cudaSuccess) return "device: pinned host allocation failed";
+        h_E_ = static_cast<long long *>(hp);
+        h_flags_ = reinterpret_cast<int *>(static_cast<char *>(hp) + be);
+    }
     energies_.assign((size_t)S * E_SLOTS, 0.0);
-    for (void *p : allocs_)
-        if (!p) return "device allocation failed";
+    if (alloc_failed_) return "device allocation failed";
     launch_derive_inputs(v_, st_);
     force_rebuild_ = true;
     std::string e = check("set-up");
@@ -1090,11 +1207,10 @@ std::string Engine::enqueue_report(double *x, double *v, double *f, long long *E
 void Engine::free_frames() {
     for (Frame &f : ring_) {
         if (f.done) cudaEventSynchronize(f.done);
-        if (f.x) cudaFreeHost(f.x);
-        if (f.E) cudaFreeHost(f.E);
-        if (f.flags) cudaFreeHost(f.flags);
         if (f.done) cudaEventDestroy(f.done);
     }
+    if (ring_mem_) cudaFreeHost(ring_mem_);
+    ring_mem_ = nullptr;
     ring_.clear();
     ring_next_ = ring_pending_ = 0;
 }
@@ -1103,14 +1219,25 @@ std::string Engine::frames_init(int depth) {
     if (depth < 1 || depth > 64) return "frame ring depth must be 1..64";
     if (ring_pending_) return "frames still pending: wait for them first";
     free_frames();
+    // one pinned allocation for all slots (pinning is slow per call):
+    // per slot the positions, the energy words and the flags, 256-byte aligned
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t bx = al(sizeof(double) * 3 * (size_t)N_), be = al(sizeof(long long) * energies_.size()),
+                 bf = al(sizeof(Flags)), slot = bx + be + bf;
+    if (cudaMallocHost(&ring_mem_, slot * depth) != cudaSuccess) {
+        ring_mem_ = nullptr;
+        return "device: pinned frame buffers could not be allocated";
+    }
     ring_.resize(depth);
-    for (Frame &f : ring_) {
-        if (cudaMallocHost(&f.x, sizeof(double) * 3 * (size_t)N_) != cudaSuccess ||
-            cudaMallocHost(&f.E, sizeof(long long) * energies_.size()) != cudaSuccess ||
-            cudaMallocHost(&f.flags, sizeof(Flags)) != cudaSuccess ||
-            cudaEventCreateWithFlags(&f.done, cudaEventDisableTiming) != cudaSuccess) {
+    for (int k = 0; k < depth; ++k) {
+        char *base = static_cast<char *>(ring_mem_) + slot * k;
+        Frame &f = ring_[k];
+        f.x = reinterpret_cast<double *>(base);
+        f.E = reinterpret_cast<long long *>(base + bx);
+        f.flags = reinterpret_cast<int *>(base + bx + be);
+        if (cudaEventCreateWithFlags(&f.done, cudaEventDisableTiming) != cudaSuccess) {
             free_frames();
-            return "device: pinned frame buffers could not be allocated";
+            return "device: frame events could not be created";
         }
     }
     return check("frames");
@@ -1174,13 +1301,13 @@ std::string Engine::compute_forces() {
     return finish_call();
 }
 
-std::string Engine::time_steps(int nsteps, double dt, double *ms) {
+std::string Engine::time_steps(int nsteps, double dt, double *ms, int report) {
     cudaEvent_t a, b;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
     cudaEventRecord(a, st_);
     for (int k = 0; k < nsteps; ++k) {
-        std::string e = one_step(dt, 0);
+        std::string e = one_step(dt, report);
         if (!e.empty()) return e;
     }
     cudaEventRecord(b, st_);

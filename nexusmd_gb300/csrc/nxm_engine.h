@@ -13,7 +13,7 @@ namespace nxm {
 
 constexpr int kProfilePhases = 8;
 constexpr int kLayoutWords = 11;
-constexpr int kCreatePhases = 6;
+constexpr int kCreatePhases = 8;
 
 struct HostSystem {
     int n = 0;
@@ -99,7 +99,9 @@ public:
     // spectrum (K0 K1 (K2/2+1)) and the real grid after the convolution and
     // inverse transform (K0 K1 K2); any pointer may be null.
     std::string pme_grids(int s, double *charge, double *influence, double *potential);
-    std::string time_steps(int nsteps, double dt, double *ms);
+    // Device milliseconds of nsteps steps (report != 0: every step computes
+    // energies and the snapshot, as a reporting loop's steps do).
+    std::string time_steps(int nsteps, double dt, double *ms, int report = 0);
     std::string profile(int nsteps, double dt, double *ms);
     int n_total() const { return N_; }
     int n_systems() const { return (int)sysh_.size(); }
@@ -120,7 +122,8 @@ public:
     // Host wall milliseconds of context creation: [0] host set-up (box,
     // constants, exclusions), [1] device allocation and uploads, [2] PME
     // tables and FFT plan, [3] autotuning (0 when skipped or cached),
-    // [4] step-graph builds so far, [5] creation total ([0]..[3]).
+    // [4] step-graph builds so far, [5] creation total ([0]..[3]); of [1]:
+    // [6] cudaMalloc and zeroing, [7] host-to-device copies.
     const double *create_ms() const { return create_ms_; }
     // 1 when the launch shapes came from an earlier context of the same shapes
     int autotune_cached() const { return autotune_cached_; }
@@ -175,12 +178,18 @@ private:
         bool pending = false;
     };
     std::vector<Frame> ring_;
+    void *ring_mem_ = nullptr;  // one pinned block holding every slot
     int ring_next_ = 0, ring_pending_ = 0;
     void free_frames();
     int autotune_cached_ = 0;
     bool force_rebuild_ = true;
     int since_rebuild_ = 0;
     std::vector<void *> allocs_;
+    // bump allocation of the engine's many small device arrays out of a few
+    // zeroed chunks (one cudaMalloc and one memset per chunk, not per array)
+    char *arena_ptr_ = nullptr;
+    size_t arena_left_ = 0;
+    bool alloc_failed_ = false;
     std::vector<double> energies_;  // [S][E_SLOTS] decoded
     long long *h_E_ = nullptr;       // pinned
     int *h_flags_ = nullptr;         // pinned

@@ -52,7 +52,7 @@ struct DevView {
     int2 *gspan_n;       // [ngroups]: (atoms, spans) of that neighbourhood
     float4 *dtab;        // [S][kDtabStride] cell-image displacement per code
     float2 *cgrid;       // per system and axis, per cell: corner's PME grid coordinate (int part, fraction)
-    double *xref;        // [3][N] positions at the last rebuild
+    double *xref;        // [3][N] positions at the last rebuild (mixed: as fix40 integers)
     float4 *oref;        // mixed: cell offsets at the last rebuild, .w = q * sqrt(ke)
     int *excl_off, *excl_lst;  // CSR by original index, partners as original indices
     // scratch used by the permutation
@@ -66,11 +66,13 @@ struct DevView {
     int4 *tors_orig, *tors_slot;
     double2 *tors_prm;   // k, phase
     int *tors_per;
+    float2 *bond_prmf, *angle_prmf, *tors_prmf;  // mixed: the same parameters in FP32
     int nex;
     int2 *ex_orig, *ex_slot;   // excluded pairs (i < j by original index)
     int nxc;                   // exception pairs (OpenMM semantics), also excluded
     int2 *xc_orig, *xc_slot;
     double4 *xc_prm;           // ke * chargeProd, sigma, 4 epsilon, 0
+    float4 *xc_prmf;           // mixed: the same in FP32
     int *bond_sys, *angle_sys, *tors_sys, *ex_sys;
     // PME
     long long total_grid, total_cgrid;

@@ -88,6 +88,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     L.nxm_get_pairs.argtypes = [C.c_void_p, C.c_int32, np.ctypeslib.ndpointer(np.int32), C.c_int64]
     L.nxm_get_pairs.restype = C.c_int64
     L.nxm_time_steps.argtypes = [C.c_void_p, C.c_int32, C.c_double, C.POINTER(C.c_double)]
+    L.nxm_time_report_steps.argtypes = [C.c_void_p, C.c_int32, C.c_double, C.POINTER(C.c_double)]
     L.nxm_profile_phases.argtypes = [C.c_void_p, C.c_int32, C.c_double, dp, C.c_int32]
     L.nxm_launches_per_step.argtypes = [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     L.nxm_rebuild_count.argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
@@ -236,6 +237,12 @@ class Engine:
         _check(self._L.nxm_time_steps(self._h, int(nsteps), float(dt), C.byref(ms)), "time_steps")
         return ms.value
 
+    def time_report_steps(self, nsteps, dt):
+        """Device milliseconds of nsteps steps that each compute energies and the snapshot."""
+        ms = C.c_double()
+        _check(self._L.nxm_time_report_steps(self._h, int(nsteps), float(dt), C.byref(ms)), "time_report_steps")
+        return ms.value
+
     def _get(self, fn):
         out = np.zeros((self.n_atoms, 3))
         _check(fn(self._h, out), fn.__name__)
@@ -316,7 +323,7 @@ class Engine:
         return q, e, r
 
     CREATE_PHASES = ("host_setup", "device_alloc_upload", "pme_tables_fft_plan", "autotune", "graph_builds",
-                     "create_total")
+                     "create_total", "of_which_alloc", "of_which_upload")
 
     def create_timing(self):
         """Host milliseconds of context creation by phase, and whether the

@@ -10,7 +10,10 @@ real grid (NonbondedForce.cpp:264-290, 323-388).  The reciprocal energy
 
 Grids: the configurations' 32^3, 64^3, 100^3 and 180^3 (passes of radix
 8, 10, 9, 6, 4, 2), and a mixed 40 x 36 x 30.  Tolerances: FP32 engine
-rel-RMS 1e-5 on the grid and 1e-5 relative on the energy; FP64 engine 1e-11.
+rel-RMS 1e-5 on the grid and 1e-5 relative on the energy; FP64 engine 1e-11
+on the grid and 1e-9 on the energy, which the engine sums per spectrum
+element as fixed point in units of 2^-28 kJ/mol (order-free, ~5e5 roundings
+at 100^3), as every FP64 energy parity test allows.
 """
 import numpy as np
 import pytest
@@ -57,8 +60,8 @@ def test_fft_convolution_matches_cufft(system, grid, prec, fft_path):
     assert np.abs(q).sum() > 0
     ref, e_ref = _cufft_reference(q, eterm)
     err = float(np.sqrt(((pot - ref) ** 2).sum() / (ref ** 2).sum()))
-    tol = 1e-5 if prec == 1 else 1e-11
+    tol, etol = (1e-5, 1e-5) if prec == 1 else (1e-11, 1e-9)
     print("grid", grid, "precision", prec, "path", fft_path, "grid rel-RMS vs cuFFT", err,
           "energy", e_recip, "cuFFT", e_ref)
     assert err <= tol, (grid, prec, err)
-    assert abs(e_recip - e_ref) <= tol * abs(e_ref), (grid, prec, e_recip, e_ref)
+    assert abs(e_recip - e_ref) <= etol * abs(e_ref), (grid, prec, e_recip, e_ref)
