@@ -1,4 +1,6 @@
 // Leapfrog update, kinetic energy and report snapshot, one thread per slot.
+// report: 0 none, 1 energies and the x/v/F snapshot, 2 energies and the
+// positions only (a frame).
 //
 // VerletIntegration::Advance (core/baseline/src/VerletIntegration.cpp:49-89)
 // with dt[0] = dt[1] = dt: v += invm F dt; x' = x + v dt; one +-L wrap into
@@ -58,11 +60,16 @@ __global__ void __launch_bounds__(256) k_integrate(DevView v, double dt, int rep
                 }
                 ke = 0.5 * m * (vh[0] * vh[0] + vh[1] * vh[1] + vh[2] * vh[2]);
             }
+            // report 1: positions, velocities and forces; report 2: a frame
+            // (positions only, into the frame buffer the view points at)
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                v.snap_x[3 * (size_t)o + c] = p[c];
-                v.snap_v[3 * (size_t)o + c] = u[c];
-                v.snap_f[3 * (size_t)o + c] = F(c);
+            for (int c = 0; c < 3; ++c) v.snap_x[3 * (size_t)o + c] = p[c];
+            if (report == 1) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    v.snap_v[3 * (size_t)o + c] = u[c];
+                    v.snap_f[3 * (size_t)o + c] = F(c);
+                }
             }
         }
         double im = v.invm[s];

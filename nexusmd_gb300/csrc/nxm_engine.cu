@@ -295,6 +295,13 @@ T *Engine::dalloc(size_t n) {
 Engine::~Engine() {
     if (st_) cudaStreamSynchronize(st_);
     free_frames();
+    for (int b = 0; b < 2; ++b) {
+        if (frame_x_[b]) cudaFree(frame_x_[b]);
+        if (frame_E_[b]) cudaFree(frame_E_[b]);
+        if (buf_free_[b]) cudaEventDestroy(buf_free_[b]);
+    }
+    if (step_done_) cudaEventDestroy(step_done_);
+    if (st_copy_) cudaStreamDestroy(st_copy_);
     free_graphs();
     for (void *p : allocs_) cudaFree(p);
     fft_plan_free(plan_);
@@ -1084,7 +1091,8 @@ std::string Engine::build_graph(double dt, int report) {
 }
 
 std::string Engine::build_graph_timed(double dt, int report) {
-    StepGraph &G = graph_[report ? 1 : 0];
+    StepGraph &G = graph_[report];
+    const DevView vv = view_for(report);
     if (G.exec) cudaGraphExecDestroy(G.exec);
     if (G.graph) cudaGraphDestroy(G.graph);
     G = StepGraph{};
@@ -1106,8 +1114,8 @@ std::string Engine::build_graph_timed(double dt, int report) {
     // head: energy reset and the decision
     e = cudaStreamBeginCaptureToGraph(st_, g, nullptr, nullptr, 0, mode);
     if (e != cudaSuccess) return fail_capture("capture head", e);
-    if (report) cudaMemsetAsync(v_.E, 0, sizeof(long long) * v_.S * E_SLOTS, st_);
-    k_decide_graph<<<1, 1, 0, st_>>>(v_, h);
+    if (report) cudaMemsetAsync(vv.E, 0, sizeof(long long) * v_.S * E_SLOTS, st_);
+    k_decide_graph<<<1, 1, 0, st_>>>(vv, h);
     cudaStreamCaptureStatus cs;
     const cudaGraphNode_t *deps = nullptr;
     size_t nd = 0;
@@ -1128,7 +1136,7 @@ std::string Engine::build_graph_timed(double dt, int report) {
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     e = cudaStreamBeginCaptureToGraph(st_, body, nullptr, nullptr, 0, mode);
     if (e != cudaSuccess) return fail_capture("capture rebuild", e);
-    launch_nlist_rebuild(v_, st_);
+    launch_nlist_rebuild(vv, st_);
     e = cudaStreamEndCapture(st_, &captured);
     if (e != cudaSuccess) return fail_capture("end rebuild", e);
     // tail: forces and update, after the conditional node
@@ -1137,10 +1145,10 @@ std::string Engine::build_graph_timed(double dt, int report) {
     // PME as a parallel branch on the second stream, joined before the update
     cudaEventRecord(ev_fork_, st_);
     cudaStreamWaitEvent(st_pme_, ev_fork_, 0);
-    force_launches(v_, plan_, report, st_, st_pme_);
+    force_launches(vv, plan_, report ? 1 : 0, st_, st_pme_);
     cudaEventRecord(ev_join_, st_pme_);
     cudaStreamWaitEvent(st_, ev_join_, 0);
-    launch_integrate(v_, dt, report, st_);
+    launch_integrate(vv, dt, report >= 2 ? 2 : report, st_);
     e = cudaStreamEndCapture(st_, &captured);
     if (e != cudaSuccess) return fail_capture("end tail", e);
     e = cudaGraphInstantiate(&G.exec, g, 0);
@@ -1150,10 +1158,12 @@ std::string Engine::build_graph_timed(double dt, int report) {
     return "";
 }
 
+// One step of report kind `report` (0 none, 1 energies and the x/v/F
+// snapshot, 2 / 3 a frame into frame buffer A / B).
 std::string Engine::one_step(double dt, int report) {
     launches_per_rebuild_ = 10;  // kernels of one list rebuild
     if (!force_rebuild_) {
-        StepGraph &G = graph_[report ? 1 : 0];
+        StepGraph &G = graph_[report];
         if (!G.ok || G.dt != dt) {
             std::string e = build_graph(dt, report);
             if (!e.empty()) return e;
@@ -1164,12 +1174,13 @@ std::string Engine::one_step(double dt, int report) {
         launches_per_step_ = force_launch_count(v_, plan_) + 2;
         return check("step");
     }
-    if (report) cudaMemsetAsync(v_.E, 0, sizeof(long long) * v_.S * E_SLOTS, st_);
-    launch_decide_rebuild(v_, 1, st_);
+    const DevView vv = view_for(report);
+    if (report) cudaMemsetAsync(vv.E, 0, sizeof(long long) * v_.S * E_SLOTS, st_);
+    launch_decide_rebuild(vv, 1, st_);
     force_rebuild_ = false;
-    launch_nlist_rebuild(v_, st_);
-    int n = force_launches(v_, plan_, report, st_);
-    launch_integrate(v_, dt, report, st_);
+    launch_nlist_rebuild(vv, st_);
+    int n = force_launches(vv, plan_, report ? 1 : 0, st_);
+    launch_integrate(vv, dt, report >= 2 ? 2 : report, st_);
     launches_per_step_ = n + 2 + launches_per_rebuild_;
     return check("step");
 }
@@ -1205,6 +1216,7 @@ std::string Engine::enqueue_report(double *x, double *v, double *f, long long *E
 }
 
 void Engine::free_frames() {
+    if (st_copy_) cudaStreamSynchronize(st_copy_);
     for (Frame &f : ring_) {
         if (f.done) cudaEventSynchronize(f.done);
         if (f.done) cudaEventDestroy(f.done);
@@ -1213,6 +1225,15 @@ void Engine::free_frames() {
     ring_mem_ = nullptr;
     ring_.clear();
     ring_next_ = ring_pending_ = 0;
+}
+
+DevView Engine::view_for(int kind) const {
+    DevView v = v_;
+    if (kind >= 2) {
+        v.E = frame_E_[kind - 2];
+        v.snap_x = frame_x_[kind - 2];
+    }
+    return v;
 }
 
 std::string Engine::frames_init(int depth) {
@@ -1227,6 +1248,19 @@ std::string Engine::frames_init(int depth) {
     if (cudaMallocHost(&ring_mem_, slot * depth) != cudaSuccess) {
         ring_mem_ = nullptr;
         return "device: pinned frame buffers could not be allocated";
+    }
+    if (!st_copy_) {
+        // device frame buffers, the copy stream and its events: once per context
+        for (int b = 0; b < 2; ++b) {
+            if (cudaMalloc(&frame_x_[b], sizeof(double) * 3 * (size_t)N_) != cudaSuccess ||
+                cudaMalloc(&frame_E_[b], sizeof(long long) * energies_.size()) != cudaSuccess ||
+                cudaEventCreateWithFlags(&buf_free_[b], cudaEventDisableTiming) != cudaSuccess)
+                return "device: frame buffers could not be allocated";
+            buf_used_[b] = false;
+        }
+        if (cudaEventCreateWithFlags(&step_done_, cudaEventDisableTiming) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&st_copy_, cudaStreamNonBlocking) != cudaSuccess)
+            return "device: frame stream could not be created";
     }
     ring_.resize(depth);
     for (int k = 0; k < depth; ++k) {
@@ -1250,14 +1284,25 @@ std::string Engine::step_async(int nsteps, double dt) {
     }
     Frame &f = ring_[ring_next_];
     if (f.pending) return "frame ring full: wait for a frame before the next nxm_step_async";
+    const int b = frame_buf_;
     for (int k = 0; k < nsteps; ++k) {
-        std::string e = one_step(dt, k == nsteps - 1);
+        const bool last = k == nsteps - 1;
+        // frame buffer b is written again only after its last copy finished
+        if (last && buf_used_[b]) cudaStreamWaitEvent(st_, buf_free_[b], 0);
+        std::string e = one_step(dt, last ? 2 + b : 0);
         if (!e.empty()) return e;
     }
-    cudaMemcpyAsync(f.x, v_.snap_x, sizeof(double) * 3 * (size_t)N_, cudaMemcpyDeviceToHost, st_);
-    cudaMemcpyAsync(f.E, v_.E, sizeof(long long) * energies_.size(), cudaMemcpyDeviceToHost, st_);
+    // the flags after the step, in stream order; then the positions and
+    // energies on the copy stream while the next step runs
     cudaMemcpyAsync(f.flags, v_.flags, sizeof(Flags), cudaMemcpyDeviceToHost, st_);
-    cudaEventRecord(f.done, st_);
+    cudaEventRecord(step_done_, st_);
+    cudaStreamWaitEvent(st_copy_, step_done_, 0);
+    cudaMemcpyAsync(f.x, frame_x_[b], sizeof(double) * 3 * (size_t)N_, cudaMemcpyDeviceToHost, st_copy_);
+    cudaMemcpyAsync(f.E, frame_E_[b], sizeof(long long) * energies_.size(), cudaMemcpyDeviceToHost, st_copy_);
+    cudaEventRecord(buf_free_[b], st_copy_);
+    cudaEventRecord(f.done, st_copy_);
+    buf_used_[b] = true;
+    frame_buf_ ^= 1;
     f.pending = true;
     ring_next_ = (ring_next_ + 1) % (int)ring_.size();
     ++ring_pending_;

@@ -141,7 +141,9 @@ private:
         double dt = 0.0;
         bool ok = false;
     };
-    StepGraph graph_[2];
+    // report kinds: 0 none, 1 energies and the x/v/F snapshot, 2 / 3 a
+    // frame (energies and positions) into frame buffer A / B
+    StepGraph graph_[4];
     // Launch shapes tuned at set-up: FFT real lines per z-pass block (0 on
     // the plane path), FFT columns per y/x-pass block, threads per
     // spread/gather block.
@@ -180,7 +182,19 @@ private:
     std::vector<Frame> ring_;
     void *ring_mem_ = nullptr;  // one pinned block holding every slot
     int ring_next_ = 0, ring_pending_ = 0;
+    // Frame steps write their energies and positions into one of two device
+    // buffers (A, B: report kinds 2, 3), alternately, so the copy of frame k
+    // on st_copy_ overlaps step k+1; a buffer is written again only after
+    // its copy has finished (buf_free_).
+    double *frame_x_[2] = {nullptr, nullptr};
+    long long *frame_E_[2] = {nullptr, nullptr};
+    cudaEvent_t buf_free_[2] = {nullptr, nullptr}, step_done_ = nullptr;
+    bool buf_used_[2] = {false, false};
+    int frame_buf_ = 0;
+    cudaStream_t st_copy_ = nullptr;
     void free_frames();
+    // the device view a step of report kind `kind` runs with
+    DevView view_for(int kind) const;
     int autotune_cached_ = 0;
     bool force_rebuild_ = true;
     int since_rebuild_ = 0;
