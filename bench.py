@@ -499,14 +499,22 @@ def e2e_run(s, v0, kw, steps):
     from nexusmd_gb300.engine import Engine
     t0 = time.perf_counter()
     eng = Engine(s, precision=1, **kw)
+    t1 = time.perf_counter()
     eng.set_velocities(v0)
+    t2 = time.perf_counter()
     eng.step_async(1, DT_PS)
     for _ in range(steps - 1):
         eng.step_async(1, DT_PS)
         eng.frame_wait(copy=False)
     eng.frame_wait(copy=False)
-    dt = time.perf_counter() - t0
+    t3 = time.perf_counter()
+    dt = t3 - t0
     create = eng.create_timing()
+    # wall milliseconds of the parts: the Python constructor (descriptor
+    # arrays + nxm_create), the velocities, the steps with their frames
+    create["wall_constructor"] = (t1 - t0) * 1e3
+    create["wall_velocities"] = (t2 - t1) * 1e3
+    create["wall_steps"] = (t3 - t2) * 1e3
     eng.close()
     return dt, create
 

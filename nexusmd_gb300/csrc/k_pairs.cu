@@ -128,7 +128,10 @@ __device__ void stage(const DevView &v, const SysDev &S, float4 *s_q, float2 *s_
 // List layout: each 256-entry chunk of an atom's list is stored transposed,
 // entry p of the chunk at position 8 * (p mod 32) + p / 32, so that lane L
 // of a warp fetches entries L, L+32, ..., L+224 with one 16-byte load.
+// An entry holds 8 times the tile index (the byte offset of the atom's LJ
+// pair in the pair kernel's staged tile; tile indices stay below 8,192).
 __device__ __forceinline__ int list_pos(int p) { return (p & ~255) | ((p & 31) << 3) | ((p >> 5) & 7); }
+constexpr int kEntryShift = 3;
 
 // ------------------------------------------------------------------ build
 
@@ -287,7 +290,7 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_build(DevView v) {
                 // past the entries so far -- a slot that a later entry
                 // overwrites or that lies beyond the list's count (never in
                 // the half being stored: at most 32 entries come per iteration)
-                buf[(((m >> lane) & 1u) ? count + __popc(m & lt) : newc + lane) & 511] = (uint16_t)k;
+                buf[(((m >> lane) & 1u) ? count + __popc(m & lt) : newc + lane) & 511] = (uint16_t)(k << kEntryShift);
                 if ((newc ^ count) >> 8) {
                     // chunk count >> 8 complete: one 16-byte store per lane
                     __syncwarp();
@@ -435,9 +438,13 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_pairs_mixed(DevView v) {
     const SysDev &S = v.sys[G.sys];
     if (!S.nb_on) return;
     int cap = v.hood_cap;
-    float4 *s_q = reinterpret_cast<float4 *>(smem);
-    float2 *s_lj = reinterpret_cast<float2 *>(s_q + cap);
-    HoodSpan *spans = reinterpret_cast<HoodSpan *>(s_lj + cap);
+    // tile: LJ pairs first (a list entry is the byte offset of its atom's
+    // pair), then positions at twice that offset past them (cap is a
+    // multiple of 32, so the positions stay 16-byte aligned)
+    float2 *s_lj = reinterpret_cast<float2 *>(smem);
+    float4 *s_q = reinterpret_cast<float4 *>(s_lj + cap);
+    HoodSpan *spans = reinterpret_cast<HoodSpan *>(s_q + cap);
+    const unsigned char *q_base = reinterpret_cast<const unsigned char *>(s_q);
     __shared__ float4 s_dt[25 * kRowCells];
     __shared__ int2 s_nn;
     int c3f = v.cell3[a0];
@@ -483,6 +490,9 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_pairs_mixed(DevView v) {
             // this lane's entries c0 + lane + 32u, u = 0..7, and the next chunk in flight
             uint4 nxt = c0 + 256 < cnt ? __ldg(lst4 + (c0 + 256) / 8) : make_uint4(0, 0, 0, 0);
             uint32_t wds[4] = {cur.x, cur.y, cur.z, cur.w};
+            // bit u: entry u's FP32 r^2 lies within 1e-5 of the cutoff, so
+            // the FP32 test (which left it out) is re-done in FP64 below
+            unsigned amb = 0;
             // FULL: all 256 entries of the chunk are valid (every chunk but
             // the last), so the per-entry range checks compile away
             auto walk = [&](auto full_chunk) {
@@ -492,23 +502,21 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_pairs_mixed(DevView v) {
                     if (!FULL && c0 + 32 * u >= cnt) break;  // rest of the last chunk is empty (warp-uniform)
                     int k0 = c0 + lane + 32 * u;
                     bool v0 = FULL || k0 < cnt, v1 = FULL || k0 + 32 < cnt;
-                    int t0 = v0 ? (int)(wds[u >> 1] & 0xffffu) : 0;
-                    int t1 = v1 ? (int)(wds[u >> 1] >> 16) : 0;
-                    float4 p0 = s_q[t0], p1 = s_q[t1];
-                    float2 l0 = s_lj[t0], l1 = s_lj[t1];
+                    const unsigned e0 = v0 ? (wds[u >> 1] & 0xffffu) : 0u;
+                    const unsigned e1 = v1 ? (wds[u >> 1] >> 16) : 0u;
+                    const float4 p0 = *reinterpret_cast<const float4 *>(q_base + 2 * e0);
+                    const float4 p1 = *reinterpret_cast<const float4 *>(q_base + 2 * e1);
+                    const float2 l0 = *reinterpret_cast<const float2 *>(smem + e0);
+                    const float2 l1 = *reinterpret_cast<const float2 *>(smem + e1);
                     // j - i: x and y as one pair per entry
                     const float2 dxy0 = __fadd2_rn(make_float2(p0.x, p0.y), nxy);
                     const float2 dxy1 = __fadd2_rn(make_float2(p1.x, p1.y), nxy);
                     const float dz0 = p0.z + nz, dz1 = p1.z + nz;
                     float r20 = v0 ? fmaf(dz0, dz0, fmaf(dxy0.y, dxy0.y, dxy0.x * dxy0.x)) : 1e30f;
                     float r21 = v1 ? fmaf(dz1, dz1, fmaf(dxy1.y, dxy1.y, dxy1.x * dxy1.x)) : 1e30f;
-                    bool in0 = r20 < lo, in1 = r21 < lo;
-                    bool b0 = !in0 && r20 < hi, b1 = !in1 && r21 < hi;
-                    if (__any_sync(full, b0 || b1)) {
-                        // within 1e-5 of the cutoff: decide in FP64 exactly as the reference
-                        if (b0) in0 = exact_r2(v, S, i, hood_slot(spans, nsp, t0)) < S.cut2;
-                        if (b1) in1 = exact_r2(v, S, i, hood_slot(spans, nsp, t1)) < S.cut2;
-                    }
+                    const bool in0 = r20 < lo, in1 = r21 < lo;
+                    amb |= ((!in0 && r20 < hi) ? 1u : 0u) << u;
+                    amb |= ((!in1 && r21 < hi) ? 1u : 0u) << (u + 1);
                     if (SW) {
                         pair_mixed<ENERGY, SW>(in0, -dxy0.x, -dxy0.y, -dz0, r20, qi * p0.w, li.x + l0.x,
                                                li.y * l0.y, P, fx, fy, fz, ec, ev);
@@ -525,6 +533,27 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_pairs_mixed(DevView v) {
                 walk(std::true_type{});
             else
                 walk(std::false_type{});
+            if (__any_sync(full, amb != 0)) {
+                // near the cutoff: decide in FP64 exactly as the reference;
+                // an entry within the cutoff is evaluated here (the walk
+                // dropped it)
+                for (int u = 0; u < 8; ++u) {
+                    if (!((amb >> u) & 1u)) continue;
+                    const unsigned e = (wds[u >> 1] >> (16 * (u & 1))) & 0xffffu;
+                    if (!(exact_r2(v, S, i, hood_slot(spans, nsp, (int)(e >> kEntryShift))) < S.cut2)) continue;
+                    const float4 pj = *reinterpret_cast<const float4 *>(q_base + 2 * e);
+                    const float2 lj = *reinterpret_cast<const float2 *>(smem + e);
+                    // j - i, the walk's convention (the sums are negated at the end)
+                    const float dx = pj.x - pi3[0], dy = pj.y - pi3[1], dz = pj.z - pi3[2];
+                    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                    if (SW)
+                        pair_mixed<ENERGY, SW>(true, -dx, -dy, -dz, r2, qi * pj.w, li.x + lj.x, li.y * lj.y, P, fx,
+                                               fy, fz, ec, ev);
+                    else
+                        pair_mixed<ENERGY, SW>(true, dx, dy, dz, r2, qi * pj.w, li.x + lj.x, li.y * lj.y, P, fxy.x,
+                                               fxy.y, fz, ec, ev);
+                }
+            }
             cur = nxt;
         }
         if (!SW) {
@@ -542,10 +571,9 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_pairs_mixed(DevView v) {
         }
     }
     if (ENERGY) {
-        if (!SW) {
-            ec = ecv.x;
-            ev = ecv.y;
-        }
+        // the packed sums, and the near-cutoff corrections (scalar)
+        ec += ecv.x;
+        ev += ecv.y;
         // each pair sits in both partners' lists
         energy_add_f(v.E, G.sys, E_COUL, 0.5f * ec);
         energy_add_f(v.E, G.sys, E_VDW, 0.5f * ev);
@@ -580,7 +608,7 @@ __global__ void __launch_bounds__(kHoodWarps * 32) k_pairs_fp64(DevView v) {
         const uint16_t *lst = v.nl16 + (size_t)i * v.stride;
         double fx = 0, fy = 0, fz = 0;
         for (int k = lane; k < cnt; k += 32) {
-            int j = hood_slot(spans, nsp, lst[list_pos(k)]);
+            int j = hood_slot(spans, nsp, lst[list_pos(k)] >> kEntryShift);
             if (!(exact_r2(v, S, i, j) < S.cut2)) continue;
             // deltaR = minimumImageVector(p_i, p_j) (NonbondedForce.cpp:548)
             double dx = min_image(xi - v.x[j], S.L[0], S.halfL[0]);
@@ -653,7 +681,7 @@ __global__ void k_collect(DevView v, int sys_sel, int *out, long long cap, unsig
         int oi = v.orig[i];
         int cnt = v.ncount[i];
         for (int k = lane; k < cnt; k += 32) {
-            int j = hood_slot(spans, nsp, v.nl16[(size_t)i * v.stride + list_pos(k)]);
+            int j = hood_slot(spans, nsp, v.nl16[(size_t)i * v.stride + list_pos(k)] >> kEntryShift);
             int oj = v.orig[j];
             if (oi <= oj) continue;
             if (!(exact_r2(v, S, i, j) < S.cut2)) continue;

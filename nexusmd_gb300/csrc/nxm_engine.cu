@@ -540,7 +540,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     v_.cell_fill = dalloc<int>(cell_off + 1);
     v_.new_orig = dalloc<int>(N_);
     hood_cap = (hood_cap + 31) / 32 * 32;
-    if (hood_cap > 65535) return "neighbourhood too dense for 16-bit list entries";
+    if (hood_cap > 8191) return "neighbourhood too dense for 16-bit list entries";
     v_.hood_cap = hood_cap;
     v_.nl16 = dalloc<uint16_t>((size_t)N_ * stride);
     {
