@@ -233,12 +233,12 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_build(DevView v) {
                 int zhi = min((int)floorf((pi3[2] + h) * icsz), g + 1);
                 if (zlo <= zhi) {
                     const int *b = s_bnd + lane * (kRowCells + 1);
-                    kb = b[zlo + 2];
-                    ke = b[zhi + 3];
                     // the row is sorted by z (cells in z order, atoms in a
-                    // cell by z): narrow to the atoms with z in pz +- h
+                    // cell by z): narrow to the atoms with z in pz +- h.  The
+                    // first such atom lies in cell zlo and the last in cell
+                    // zhi, so each search covers one cell.
                     const float zl = pi3[2] - h, zh = pi3[2] + h;
-                    int l = kb, r = ke;
+                    int l = b[zlo + 2], r = b[zlo + 3];
                     while (l < r) {
                         int mid = (l + r) >> 1;
                         if (s_q[mid].z < zl)
@@ -247,7 +247,8 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_build(DevView v) {
                             r = mid;
                     }
                     kb = l;
-                    r = ke;
+                    l = max(b[zhi + 2], kb);
+                    r = b[zhi + 3];
                     while (l < r) {
                         int mid = (l + r) >> 1;
                         if (s_q[mid].z <= zh)

@@ -6,8 +6,10 @@
 // t = (t - floor t) K, index = int(t) mod K, fraction = t - int(t) -- the
 // grid is anchored at the origin, not at the box's lower bound.  Spline
 // weights and derivatives follow computeBSplineParameters (:144-182); the
-// spread is :220-260 and the gather :407-461.  In mixed mode the weights are
-// FP32 and the grid is summed as int64 fixed point (bit-reproducible).
+// spread is :220-260 and the gather :407-461 (its sums regrouped per stencil
+// row: the z sums first, then the row's x/y weights).  In mixed mode the
+// weights are FP32 and the grid is summed as int64 fixed point
+// (bit-reproducible).
 #include <algorithm>
 
 #include "nxm_fft.h"
@@ -221,6 +223,13 @@ __global__ void __launch_bounds__(256) k_gather(DevView v, const FftSysDev *fs) 
     for (int d = 0; d < 3; ++d) bspline5<R>(fr[d], th[d], dth[d]);
     const R *g = static_cast<const R *>(v.grid_real) + F.roff;
     int K1 = F.K[1], K2 = F.K[2];
+    // the five z indices of the stencil, wrapped once
+    int zo[5];
+#pragma unroll
+    for (int iz = 0; iz < 5; ++iz) {
+        const int zi = id.z + iz;
+        zo[iz] = zi >= K2 ? zi - K2 : zi;
+    }
     R fx = 0, fy = 0, fz = 0;
 #pragma unroll
     for (int ix = 0; ix < 5; ++ix) {
@@ -231,18 +240,19 @@ __global__ void __launch_bounds__(256) k_gather(DevView v, const FftSysDev *fs) 
             int yi = id.y + iy;
             yi -= yi >= K1 ? K1 : 0;
             const R *row = g + ((long long)xi * K1 + yi) * K2;
-            R txy = th[0][ix] * th[1][iy];
-            R dxy = dth[0][ix] * th[1][iy];
-            R tdy = th[0][ix] * dth[1][iy];
+            // the row's two z sums, sum_z theta_z g and sum_z dtheta_z g, then
+            // the row's x/y weights once: (dx ty, tx dy, tx ty) applied to them
+            R sz = 0, sdz = 0;
 #pragma unroll
             for (int iz = 0; iz < 5; ++iz) {
-                int zi = id.z + iz;
-                zi -= zi >= K2 ? K2 : 0;
-                R gv = row[zi];
-                fx += dxy * th[2][iz] * gv;
-                fy += tdy * th[2][iz] * gv;
-                fz += txy * dth[2][iz] * gv;
+                const R gv = row[zo[iz]];
+                sz += th[2][iz] * gv;
+                sdz += dth[2][iz] * gv;
             }
+            const R ty = th[1][iy], dy = dth[1][iy];
+            fx += (dth[0][ix] * ty) * sz;
+            fy += (th[0][ix] * dy) * sz;
+            fz += (th[0][ix] * ty) * sdz;
         }
     }
     R q = (R)v.q[s];

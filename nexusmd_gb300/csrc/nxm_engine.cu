@@ -162,49 +162,88 @@ static std::string exclusion_rows(const HostSystem &s, int off, std::vector<int>
         }
         for (int i = 0; i < n; ++i) std::sort(xadj.begin() + xoff[i], xadj.begin() + xoff[i + 1]);
     }
-    std::vector<int> dist(n, -1), queue, row;
-    queue.reserve(64);
-    row.reserve(64);
-    for (int i = 0; i < n; ++i) {
-        row.clear();
-        if (s.excl_depth >= 1) {
-            queue.clear();
-            queue.push_back(i);
-            dist[i] = 0;
-            for (size_t h = 0; h < queue.size(); ++h) {
-                int u = queue[h];
-                if (dist[u] == s.excl_depth) continue;
-                for (int k = aoff[u]; k < aoff[u + 1]; ++k) {
-                    int w = adj[k];
-                    if (dist[w] < 0) {
-                        dist[w] = dist[u] + 1;
+    // one breadth-first search per atom; atoms split into contiguous ranges
+    // over the host's threads, each range's rows and pairs appended in
+    // order afterwards (the same CSR as one pass)
+    struct Part {
+        std::vector<int> len, lst;
+        std::vector<int2> pairs;
+    };
+    const int nth = n < 16384 ? 1 : std::max(1, std::min(8, (int)std::thread::hardware_concurrency()));
+    std::vector<Part> parts(nth);
+    auto run = [&](int t) {
+        const int i0 = (int)((long long)n * t / nth), i1 = (int)((long long)n * (t + 1) / nth);
+        Part &P = parts[t];
+        P.len.reserve(i1 - i0);
+        P.lst.reserve((size_t)(i1 - i0) * 4);
+        // the search's queue with each atom's depth; a depth-limited search
+        // visits a few dozen atoms at most, so "visited" is a scan of it
+        std::vector<int> queue, depth, row;
+        queue.reserve(64);
+        depth.reserve(64);
+        row.reserve(64);
+        for (int i = i0; i < i1; ++i) {
+            row.clear();
+            if (s.excl_depth >= 1) {
+                queue.clear();
+                depth.clear();
+                queue.push_back(i);
+                depth.push_back(0);
+                for (size_t h = 0; h < queue.size(); ++h) {
+                    const int u = queue[h], du = depth[h];
+                    if (du == s.excl_depth) continue;
+                    for (int k = aoff[u]; k < aoff[u + 1]; ++k) {
+                        const int w = adj[k];
+                        if (std::find(queue.begin(), queue.end(), w) != queue.end()) continue;
                         queue.push_back(w);
+                        depth.push_back(du + 1);
                         row.push_back(w);
                     }
                 }
+                std::sort(row.begin(), row.end());
             }
-            for (int u : queue) dist[u] = -1;
-            std::sort(row.begin(), row.end());
-        }
-        // sorted union with the exception partners
-        const size_t base = elst.size();
-        size_t p = 0;
-        int q = xoff[i];
-        while (p < row.size() || q < xoff[i + 1]) {
-            int v;
-            if (q >= xoff[i + 1] || (p < row.size() && row[p] < xadj[q]))
-                v = row[p++];
-            else if (p >= row.size() || xadj[q] < row[p])
-                v = xadj[q++];
-            else {
-                v = row[p++];
-                ++q;
+            // sorted union with the exception partners
+            const size_t base = P.lst.size();
+            size_t p = 0;
+            int q = xoff[i];
+            while (p < row.size() || q < xoff[i + 1]) {
+                int v;
+                if (q >= xoff[i + 1] || (p < row.size() && row[p] < xadj[q]))
+                    v = row[p++];
+                else if (p >= row.size() || xadj[q] < row[p])
+                    v = xadj[q++];
+                else {
+                    v = row[p++];
+                    ++q;
+                }
+                if (P.lst.size() > base && P.lst.back() == off + v) continue;  // repeated exception pair
+                P.lst.push_back(off + v);
+                if (v > i) P.pairs.push_back(make_int2(off + i, off + v));
             }
-            if (elst.size() > base && elst.back() == off + v) continue;  // repeated exception pair
-            elst.push_back(off + v);
-            if (v > i) ex_pairs.push_back(make_int2(off + i, off + v));
+            P.len.push_back((int)(P.lst.size() - base));
         }
-        eoff.push_back((int)elst.size());
+    };
+    if (nth == 1) {
+        run(0);
+    } else {
+        std::vector<std::thread> pool;
+        for (int t = 1; t < nth; ++t) pool.emplace_back(run, t);
+        run(0);
+        for (auto &th : pool) th.join();
+    }
+    size_t nl = 0, np = 0;
+    for (const Part &P : parts) {
+        nl += P.lst.size();
+        np += P.pairs.size();
+    }
+    eoff.reserve(eoff.size() + n);
+    elst.reserve(elst.size() + nl);
+    ex_pairs.reserve(ex_pairs.size() + np);
+    for (const Part &P : parts) {
+        int e = eoff.back();
+        for (int l : P.len) eoff.push_back(e += l);
+        elst.insert(elst.end(), P.lst.begin(), P.lst.end());
+        ex_pairs.insert(ex_pairs.end(), P.pairs.begin(), P.pairs.end());
     }
     return "";
 }
@@ -355,6 +394,28 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     double skin = opt.skin > 0 ? opt.skin : 0.0;
     int stride = 0, hood_cap = 0;
     std::vector<int> group_g(S, 1);
+    // The exclusion sets (a host-side breadth-first search per atom) do not
+    // depend on anything the device set-up below needs, so they are built on
+    // a second host thread while the device memory is allocated and filled;
+    // the thread is joined before their first use.
+    std::string ex_err;
+    struct Joiner {
+        std::thread t;
+        ~Joiner() {
+            if (t.joinable()) t.join();
+        }
+    } ex_job;
+    ex_job.t = std::thread([&systems, &eoff, &elst, &ex_pairs, &ex_err] {
+        int o = 0;
+        for (const HostSystem &h : systems) {
+            std::string e = exclusion_rows(h, o, eoff, elst, ex_pairs);
+            if (!e.empty()) {
+                ex_err = e;
+                return;
+            }
+            o += h.n;
+        }
+    });
     for (int s = 0; s < S; ++s) {
         const HostSystem &h = systems[s];
         SysDev &D = sysd_[s];
@@ -466,8 +527,6 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
                 xc_prm.push_back(make_double4(kOne4PiEps0 * p[0], p[1], 4.0 * p[2], 0.0));
             }
         }
-        std::string err = exclusion_rows(h, off, eoff, elst, ex_pairs);
-        if (!err.empty()) return err;
         // list capacity from the density
         double vol = H.L[0] * H.L[1] * H.L[2];
         double expect = 4.0 / 3.0 * kPi * H.rlist * H.rlist * H.rlist * h.n / vol;
@@ -643,7 +702,9 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         up(v_.cgrid, cg.data(), sizeof(float2) * cg.size());
     }
 
-    // exclusion CSR (batch-global original indices), built per system above
+    // exclusion CSR (batch-global original indices), from the host thread
+    ex_job.t.join();
+    if (!ex_err.empty()) return ex_err;
     v_.excl_off = dalloc<int>(N_ + 1);
     v_.excl_lst = dalloc<int>(elst.size());
     up(v_.excl_off, eoff.data(), sizeof(int) * (N_ + 1));
