@@ -235,10 +235,11 @@ int nxm_get_pme_grids(nxm_ctx *ctx, int32_t system, double *charge, double *infl
  * and FFT plan, [3] autotuning of launch shapes (about 0 when autotune is
  * off or an earlier context of the same shapes in this process was tuned:
  * *autotune_cached = 1), [4] step-graph builds so far (the first steps
- * build them), [5] the creation total [0] + [1] + [2] + [3]; and, within
- * [1], [6] device allocation with zeroing and [7] host-to-device copies.  The
- * reference builds its Engine per Simulate call (Engine.cpp:19-73). */
-int nxm_get_create_timing(nxm_ctx *ctx, double ms[8], int32_t *autotune_cached);
+ * build them), [5] the creation total [0] + [1] + [2] + [3]; within [1],
+ * [6] device allocation with zeroing and [7] host-to-device copies; [8] the
+ * exclusion sets, built on host threads while [1] runs.  The reference
+ * builds its Engine per Simulate call (Engine.cpp:19-73). */
+int nxm_get_create_timing(nxm_ctx *ctx, double ms[9], int32_t *autotune_cached);
 
 /* Layout of one system of the context: [0] cells per cell group (one block
  * of the list-build and pair kernels per group), [1] atoms a staged

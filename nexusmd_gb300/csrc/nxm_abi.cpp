@@ -269,7 +269,7 @@ int nxm_frame_wait(nxm_ctx *ctx, const double **xyz, nxm_energies *energies, int
     NXM_CALL(ctx->eng.frame_wait(xyz, energies, n_systems));
 }
 
-int nxm_get_create_timing(nxm_ctx *ctx, double ms[8], int32_t *autotune_cached) {
+int nxm_get_create_timing(nxm_ctx *ctx, double ms[9], int32_t *autotune_cached) {
     if (!ctx || !ms) return fail(NXM_ERR_INVALID, "null argument");
     const double *c = ctx->eng.create_ms();
     for (int k = 0; k < nxm::kCreatePhases; ++k) ms[k] = c[k];

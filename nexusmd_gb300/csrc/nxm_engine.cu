@@ -169,7 +169,7 @@ static std::string exclusion_rows(const HostSystem &s, int off, std::vector<int>
         std::vector<int> len, lst;
         std::vector<int2> pairs;
     };
-    const int nth = n < 16384 ? 1 : std::max(1, std::min(8, (int)std::thread::hardware_concurrency()));
+    const int nth = n < 16384 ? 1 : std::max(1, std::min(15, (int)std::thread::hardware_concurrency() - 1));
     std::vector<Part> parts(nth);
     auto run = [&](int t) {
         const int i0 = (int)((long long)n * t / nth), i1 = (int)((long long)n * (t + 1) / nth);
@@ -405,16 +405,18 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
             if (t.joinable()) t.join();
         }
     } ex_job;
-    ex_job.t = std::thread([&systems, &eoff, &elst, &ex_pairs, &ex_err] {
+    ex_job.t = std::thread([this, &systems, &eoff, &elst, &ex_pairs, &ex_err] {
+        const double t0 = now_ms();
         int o = 0;
         for (const HostSystem &h : systems) {
             std::string e = exclusion_rows(h, o, eoff, elst, ex_pairs);
             if (!e.empty()) {
                 ex_err = e;
-                return;
+                break;
             }
             o += h.n;
         }
+        create_ms_[8] = now_ms() - t0;
     });
     for (int s = 0; s < S; ++s) {
         const HostSystem &h = systems[s];

@@ -13,7 +13,7 @@ namespace nxm {
 
 constexpr int kProfilePhases = 8;
 constexpr int kLayoutWords = 11;
-constexpr int kCreatePhases = 8;
+constexpr int kCreatePhases = 9;
 
 struct HostSystem {
     int n = 0;
@@ -123,7 +123,8 @@ public:
     // constants, exclusions), [1] device allocation and uploads, [2] PME
     // tables and FFT plan, [3] autotuning (0 when skipped or cached),
     // [4] step-graph builds so far, [5] creation total ([0]..[3]); of [1]:
-    // [6] cudaMalloc and zeroing, [7] host-to-device copies.
+    // [6] cudaMalloc and zeroing, [7] host-to-device copies; [8] the
+    // exclusion sets, built on a host thread alongside [1].
     const double *create_ms() const { return create_ms_; }
     // 1 when the launch shapes came from an earlier context of the same shapes
     int autotune_cached() const { return autotune_cached_; }
