@@ -152,7 +152,10 @@ __device__ __forceinline__ void store_chunk(uint16_t *dst, const uint16_t *src, 
     reinterpret_cast<uint4 *>(dst)[lane] = make_uint4(w[0], w[1], w[2], w[3]);
 }
 
-__global__ void __launch_bounds__(kHoodWarps * 32, 2) k_build(DevView v) {
+// W warps per block: 16 (two blocks per SM) or, when two blocks' shared
+// memory does not fit on an SM, 32 (one block per SM, the same 32 warps).
+template <int W>
+__global__ void __launch_bounds__(W * 32, W == kHoodWarps ? 2 : 1) k_build(DevView v) {
     extern __shared__ __align__(16) unsigned char smem[];
     if (!v.flags->rebuild) return;
     const unsigned full = 0xffffffffu;
@@ -167,8 +170,8 @@ __global__ void __launch_bounds__(kHoodWarps * 32, 2) k_build(DevView v) {
     int cap = v.hood_cap;
     float4 *s_q = reinterpret_cast<float4 *>(smem);
     int *s_orig = reinterpret_cast<int *>(s_q + cap);
-    uint16_t *s_buf = reinterpret_cast<uint16_t *>(s_orig + cap);  // [kHoodWarps][2][256], 16-byte aligned
-    int *s_bnd = reinterpret_cast<int *>(s_buf + kHoodWarps * 512);
+    uint16_t *s_buf = reinterpret_cast<uint16_t *>(s_orig + cap);  // [W][2][256], 16-byte aligned
+    int *s_bnd = reinterpret_cast<int *>(s_buf + W * 512);
     HoodSpan *spans = reinterpret_cast<HoodSpan *>(s_bnd + 25 * (kRowCells + 1));
     int *s_n = reinterpret_cast<int *>(spans + kMaxSpans);
     __shared__ float4 s_dt[25 * kRowCells];
@@ -429,8 +432,8 @@ __device__ __forceinline__ void pair_mixed2(bool in0, bool in1, float2 dxy0, flo
 
 // Mixed precision: each lane keeps two list entries in flight; j comes from
 // the staged tile.  SW: some system of the batch uses the switching function.
-template <bool ENERGY, bool SW>
-__global__ void __launch_bounds__(kHoodWarps * 32, 2) k_pairs_mixed(DevView v) {
+template <bool ENERGY, bool SW, int W>
+__global__ void __launch_bounds__(W * 32, W == kHoodWarps ? 2 : 1) k_pairs_mixed(DevView v) {
     extern __shared__ __align__(16) unsigned char smem[];
     const unsigned full = 0xffffffffu;
     CellGroup G = v.groups[blockIdx.x];
@@ -698,12 +701,30 @@ __global__ void k_collect(DevView v, int sys_sel, int *out, long long cap, unsig
 // ------------------------------------------------------------------ launch
 
 static size_t tail_bytes() { return kMaxSpans * sizeof(HoodSpan) + 4 * sizeof(int); }
-static size_t smem_build(int cap) {
-    return (size_t)cap * (sizeof(float4) + sizeof(int)) + kHoodWarps * 512 * sizeof(uint16_t) +
+static size_t smem_build(int cap, int warps) {
+    return (size_t)cap * (sizeof(float4) + sizeof(int)) + (size_t)warps * 512 * sizeof(uint16_t) +
            25 * (kRowCells + 1) * sizeof(int) + tail_bytes();
 }
 static size_t smem_pairs(int cap, int mixed) {
     return mixed ? (size_t)cap * (sizeof(float4) + sizeof(float2)) + tail_bytes() : tail_bytes();
+}
+// static shared memory of the tile kernels (displacement table and counts)
+constexpr size_t kTileStatic = 25 * kRowCells * sizeof(float4) + 16;
+
+// Two blocks of 16 warps per SM when both blocks' shared memory fits (228 KB
+// per SM, 1 KB reserved per block); otherwise one block of 32 warps, which
+// keeps 32 warps on the SM at the same 64 registers per thread.  (Dense
+// neighbourhoods -- one-cell groups of large cells -- need the latter.)
+static bool wide(size_t dynamic_smem) { return 2 * (dynamic_smem + kTileStatic + 1024) > 228 * 1024; }
+static int build_warps(int cap) { return wide(smem_build(cap, kHoodWarps)) ? 2 * kHoodWarps : kHoodWarps; }
+static int pair_warps(int cap) { return wide(smem_pairs(cap, 1)) ? 2 * kHoodWarps : kHoodWarps; }
+
+template <int W>
+static void set_pairs_smem(int m) {
+    cudaFuncSetAttribute(k_pairs_mixed<true, false, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_pairs_mixed<false, false, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_pairs_mixed<true, true, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_pairs_mixed<false, true, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
 }
 
 // The dynamic shared-memory limit is a per-kernel attribute shared by every
@@ -711,52 +732,72 @@ static size_t smem_pairs(int cap, int mixed) {
 // with a smaller neighbourhood cannot lower it under another one.
 void tiles_set_smem(int cap) {
     static std::mutex mu;
-    static int seen_build[kMaxSmemDevices] = {}, seen_pairs[kMaxSmemDevices] = {};
+    static int seen_build[2][kMaxSmemDevices] = {}, seen_pairs[2][kMaxSmemDevices] = {};
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= kMaxSmemDevices) dev = 0;
-    int b = (int)smem_build(cap), m = (int)smem_pairs(cap, 1);
+    const int bw = build_warps(cap), pw = pair_warps(cap);
+    const int b = (int)smem_build(cap, bw), m = (int)smem_pairs(cap, 1);
+    const int bi = bw == kHoodWarps ? 0 : 1, pi = pw == kHoodWarps ? 0 : 1;
     std::lock_guard<std::mutex> lock(mu);
     // launches up to 48 KB need no attribute
-    if (b > 48 * 1024 && b > seen_build[dev]) {
-        cudaFuncSetAttribute(k_build, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
-        seen_build[dev] = b;
+    if (b > 48 * 1024 && b > seen_build[bi][dev]) {
+        if (bi)
+            cudaFuncSetAttribute(k_build<2 * kHoodWarps>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+        else
+            cudaFuncSetAttribute(k_build<kHoodWarps>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+        seen_build[bi][dev] = b;
     }
-    if (m > 48 * 1024 && m > seen_pairs[dev]) {
-        cudaFuncSetAttribute(k_pairs_mixed<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-        cudaFuncSetAttribute(k_pairs_mixed<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-        cudaFuncSetAttribute(k_pairs_mixed<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-        cudaFuncSetAttribute(k_pairs_mixed<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-        seen_pairs[dev] = m;
+    if (m > 48 * 1024 && m > seen_pairs[pi][dev]) {
+        if (pi)
+            set_pairs_smem<2 * kHoodWarps>(m);
+        else
+            set_pairs_smem<kHoodWarps>(m);
+        seen_pairs[pi][dev] = m;
     }
 }
 
 void launch_build(const DevView &v, cudaStream_t st) {
-    if (v.ngroups) k_build<<<v.ngroups, kHoodWarps * 32, smem_build(v.hood_cap), st>>>(v);
+    if (!v.ngroups) return;
+    if (build_warps(v.hood_cap) == kHoodWarps)
+        k_build<kHoodWarps><<<v.ngroups, kHoodWarps * 32, smem_build(v.hood_cap, kHoodWarps), st>>>(v);
+    else
+        k_build<2 * kHoodWarps>
+            <<<v.ngroups, 2 * kHoodWarps * 32, smem_build(v.hood_cap, 2 * kHoodWarps), st>>>(v);
+}
+
+template <int W>
+static void launch_pairs_mixed(const DevView &v, int energy, cudaStream_t st) {
+    const int g = v.ngroups, t = W * 32;
+    const size_t sm = smem_pairs(v.hood_cap, 1);
+    if (v.any_switch) {
+        if (energy)
+            k_pairs_mixed<true, true, W><<<g, t, sm, st>>>(v);
+        else
+            k_pairs_mixed<false, true, W><<<g, t, sm, st>>>(v);
+    } else {
+        if (energy)
+            k_pairs_mixed<true, false, W><<<g, t, sm, st>>>(v);
+        else
+            k_pairs_mixed<false, false, W><<<g, t, sm, st>>>(v);
+    }
 }
 
 void launch_pairs(const DevView &v, int energy, cudaStream_t st) {
     if (v.N == 0 || v.ngroups == 0) return;
-    int g = v.ngroups, t = kHoodWarps * 32;
-    size_t sm = smem_pairs(v.hood_cap, v.mixed);
     if (v.mixed) {
-        if (v.any_switch) {
-            if (energy)
-                k_pairs_mixed<true, true><<<g, t, sm, st>>>(v);
-            else
-                k_pairs_mixed<false, true><<<g, t, sm, st>>>(v);
-        } else {
-            if (energy)
-                k_pairs_mixed<true, false><<<g, t, sm, st>>>(v);
-            else
-                k_pairs_mixed<false, false><<<g, t, sm, st>>>(v);
-        }
-    } else {
-        if (energy)
-            k_pairs_fp64<true><<<g, t, sm, st>>>(v);
+        if (pair_warps(v.hood_cap) == kHoodWarps)
+            launch_pairs_mixed<kHoodWarps>(v, energy, st);
         else
-            k_pairs_fp64<false><<<g, t, sm, st>>>(v);
+            launch_pairs_mixed<2 * kHoodWarps>(v, energy, st);
+        return;
     }
+    int g = v.ngroups, t = kHoodWarps * 32;
+    size_t sm = smem_pairs(v.hood_cap, 0);
+    if (energy)
+        k_pairs_fp64<true><<<g, t, sm, st>>>(v);
+    else
+        k_pairs_fp64<false><<<g, t, sm, st>>>(v);
 }
 
 long long launch_collect_pairs(const DevView &v, int sys, int *out_pairs, long long cap, cudaStream_t st) {
