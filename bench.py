@@ -635,7 +635,7 @@ def native(args):
                 gbs = b / (ph[k] * 1e-3) / 1e9
                 hbm[k] = {"achieved": sig(gbs), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                           "frac": sig(gbs / peaks["hbm_gbs"]), "bytes_per_launch": b}
-        # the spread is bound by L2 atomic throughput, not HBM: 125 int64
+        # the spread is bound by L2 atomic throughput, not HBM: 125 int32
         # atomic adds per atom against the probe's rate for the same pattern
         import ctypes as C
         rate = C.c_double()
@@ -643,7 +643,7 @@ def native(args):
             ach = 125.0 * s.n / (ph["spread"] * 1e-3)
             hbm["spread"]["l2_atomics"] = {"achieved": sig(ach), "peak": sig(rate.value), "unit": "atomics/s",
                                            "frac": sig(ach / rate.value),
-                                           "peak_source": "int64 atomic adds in 5^3 stencils at random places "
+                                           "peak_source": "int32 atomic adds in 5^3 stencils at random places "
                                                           "of a %d^3 grid (bench_probe.cu), measured here"
                                                           % s.grid[0]}
         u64, u32 = shared_atomics_probe(local)

@@ -7,7 +7,7 @@
 // as one packed FP32x2 FFMA per pair (__ffma2_rn); the launch covers every SM
 // many times over, and the rate is timed with CUDA events on its own stream.
 //
-// nxm_probe_stencil_atomics: global int64 atomic adds per second in the PME
+// nxm_probe_stencil_atomics: global int32 atomic adds per second in the PME
 // spread's pattern, the L2-atomic ceiling the spread kernel runs against.
 //
 // nxm_probe_shared_atomics: throughput of shared-memory integer atomic adds,
@@ -82,10 +82,10 @@ __global__ void __launch_bounds__(512) k_atomic_probe(unsigned long long *out, i
 }
 
 // The PME spread's global access pattern at full rate: each warp adds
-// int64 words to the 32 consecutive points (x-major, z fastest) of one 5^3
+// int32 words (the mixed engine's grid word) to the 32 consecutive points (x-major, z fastest) of one 5^3
 // stencil of a K^3 grid, at a stencil base drawn at random with every point
 // inside the grid.  One launch does `reps` stencils per warp.
-__global__ void __launch_bounds__(256) k_stencil_atomic_probe(unsigned long long *grid, int K, int reps) {
+__global__ void __launch_bounds__(256) k_stencil_atomic_probe(unsigned *grid, int K, int reps) {
     const unsigned lane = threadIdx.x & 31;
     const unsigned gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     for (int r = 0; r < reps; ++r) {
@@ -94,14 +94,14 @@ __global__ void __launch_bounds__(256) k_stencil_atomic_probe(unsigned long long
                   bz = (int)((h >> 16) % (unsigned)(K - 4));
         for (int p = (int)lane; p < 125; p += 32) {
             const int ix = p / 25, iy = (p / 5) % 5, iz = p % 5;
-            atomicAdd(&grid[((size_t)(bx + ix) * K + (by + iy)) * K + (bz + iz)], 1ull);
+            atomicAdd(&grid[((size_t)(bx + ix) * K + (by + iy)) * K + (bz + iz)], 1u);
         }
     }
 }
 
 }  // namespace nxm
 
-// Global int64 atomic adds per second in the spread's pattern (5^3 stencils
+// Global int32 atomic adds per second in the spread's pattern (5^3 stencils
 // at random places of a K^3 grid, consecutive stencil points per warp).
 extern "C" int nxm_probe_stencil_atomics(int32_t device, int32_t K, double *atomics_per_s) {
     using namespace nxm;
@@ -112,9 +112,9 @@ extern "C" int nxm_probe_stencil_atomics(int32_t device, int32_t K, double *atom
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     const size_t pts = (size_t)K * K * K;
-    unsigned long long *grid = nullptr;
-    if (cudaMalloc(&grid, sizeof(unsigned long long) * pts) != cudaSuccess) return NXM_PROBE_ERR_CUDA;
-    cudaMemset(grid, 0, sizeof(unsigned long long) * pts);
+    unsigned *grid = nullptr;
+    if (cudaMalloc(&grid, sizeof(unsigned) * pts) != cudaSuccess) return NXM_PROBE_ERR_CUDA;
+    cudaMemset(grid, 0, sizeof(unsigned) * pts);
     cudaStream_t st;
     cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
     cudaEvent_t e0, e1;

@@ -258,15 +258,9 @@ __device__ __forceinline__ void rounds(int total, Load load, Store store) {
 }
 constexpr int kRounds = 4;
 
-// Fixed-point grid word (units of 2^-32) to float without the FP64 pipe:
-// g = hi * 2^24 + lo with lo in [0, 2^24) splits it into two floats that are
-// exact (|g| < 2^47), and their sum is rounded once -- the same float as
-// (float)((double)g * 2^-32).
-__device__ __forceinline__ float grid_value(long long g) {
-    float hi = __int2float_rn((int)(g >> 24)) * 0.00390625f;                         // * 2^-8
-    float lo = __uint2float_rn((unsigned)(g & 0xffffff)) * 2.3283064365386963e-10f;  // * 2^-32
-    return hi + lo;
-}
+// Fixed-point grid word (int32, units of 2^-24) to float: one rounding, the
+// same float as (float)((double)g * 2^-24).
+__device__ __forceinline__ float grid_value(int g) { return __int2float_rn(g) * 5.9604644775390625e-08f; }
 __device__ __forceinline__ double grid_value(double g) { return g; }
 
 // Copies the twiddle table of length n at `off` into shared memory (the
@@ -620,7 +614,7 @@ static void run(const DevView &v, const FftPlan &p, int energy, cudaStream_t st)
 
 void launch_fft_convolve(const DevView &v, const FftPlan &p, int energy, cudaStream_t st) {
     if (v.mixed)
-        run<float2, long long, float>(v, p, energy, st);
+        run<float2, int, float>(v, p, energy, st);
     else
         run<double2, double, double>(v, p, energy, st);
 }
@@ -744,7 +738,7 @@ void fft_plan_build(FftPlan &p, int mixed) {
     cudaMemcpy(p.xwork, x.data(), sizeof(FftWork) * p.nx, cudaMemcpyHostToDevice);
     cudaMemcpy(p.pwork, pl.data(), sizeof(FftWork) * p.npl, cudaMemcpyHostToDevice);
     if (mixed)
-        raise_all<float2, long long, float>(p, 0);
+        raise_all<float2, int, float>(p, 0);
     else
         raise_all<double2, double, double>(p, 8);
 }

@@ -19,13 +19,14 @@ constexpr double kSqrtPi = 1.77245385090551602729;
 constexpr double kTwoOverSqrtPi = 1.1283791670955126;
 constexpr double kOne4PiEps0 = 138.93545764446428693393;
 
-// Fixed-point scales.  Forces and the mixed-precision charge grid are summed
-// as int64 multiples of 2^-32 (order-independent, so bit-reproducible);
-// energies as multiples of 2^-28 kJ/mol (|E| < 3.4e10).
+// Fixed-point scales (integer sums are order-independent, so
+// bit-reproducible).  Forces: int64 multiples of 2^-32; the mixed-precision
+// charge grid: int32 multiples of 2^-24 e; energies: int64 multiples of
+// 2^-28 kJ/mol (|E| < 3.4e10).
 constexpr double kForceScale = 4294967296.0;
 constexpr double kForceUnscale = 1.0 / 4294967296.0;
-constexpr double kGridScale = 4294967296.0;
-constexpr double kGridUnscale = 1.0 / 4294967296.0;
+constexpr double kGridScale = 16777216.0;
+constexpr double kGridUnscale = 1.0 / 16777216.0;
 constexpr double kEnergyScale = 268435456.0;
 constexpr double kEnergyUnscale = 1.0 / 268435456.0;
 

@@ -822,7 +822,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     v_.total_grid = roff;
     v_.total_cgrid = coff;
     if (any_nb) {
-        v_.grid_acc = mixed_ ? (void *)dalloc<long long>(roff) : (void *)dalloc<double>(roff);
+        v_.grid_acc = mixed_ ? (void *)dalloc<int>(roff) : (void *)dalloc<double>(roff);
         v_.grid_real = mixed_ ? (void *)dalloc<float>(roff) : (void *)dalloc<double>(roff);
         v_.grid_cplx = mixed_ ? (void *)dalloc<float2>(coff) : (void *)dalloc<double2>(coff);
         v_.eterm = mixed_ ? (void *)dalloc<float>(coff) : (void *)dalloc<double>(coff);
@@ -1558,11 +1558,11 @@ std::string Engine::pme_grids(int s, double *charge, double *influence, double *
     };
     std::vector<unsigned char> h;
     if (charge) {
-        if (fetch(v_.grid_acc, F.roff, nr, 8, h) != cudaSuccess) return check("pme_grids");
+        if (fetch(v_.grid_acc, F.roff, nr, mixed_ ? 4 : 8, h) != cudaSuccess) return check("pme_grids");
         for (size_t k = 0; k < nr; ++k) {
             if (mixed_) {
-                long long w;
-                std::memcpy(&w, &h[8 * k], 8);
+                int w;
+                std::memcpy(&w, &h[4 * k], 4);
                 charge[k] = (double)w * kGridUnscale;
             } else {
                 std::memcpy(&charge[k], &h[8 * k], 8);
