@@ -236,8 +236,8 @@ int nxm_get_pme_grids(nxm_ctx *ctx, int32_t system, double *charge, double *infl
  * off or an earlier context of the same shapes in this process was tuned:
  * *autotune_cached = 1), [4] step-graph builds so far (the first steps
  * build them), [5] the creation total [0] + [1] + [2] + [3]; within [1],
- * [6] device allocation with zeroing and [7] host-to-device copies; [8] the
- * exclusion sets, built on host threads while [1] runs.  The reference
+ * [6] device allocation with zeroing and [7] host-to-device copies, and [8]
+ * the exclusion sets (built on the device, part of [1]).  The reference
  * builds its Engine per Simulate call (Engine.cpp:19-73). */
 int nxm_get_create_timing(nxm_ctx *ctx, double ms[9], int32_t *autotune_cached);
 
@@ -327,7 +327,7 @@ int nxm_dispatcher_simulate(nxm_dispatcher *d, const char *system_xml, const cha
  *   energy   1 double, kJ/mol (overwritten: reciprocal energy)
  * Host arguments: box corners (box edge = |ub - lb|; the grid is anchored at
  * the origin as in the reference), grid sizes, Ewald alpha (1/nm).
- * All intermediates live in one static device array of about 4.8 MB per
+ * All intermediates live in one static device array of about 3.7 MB per
  * device, so each grid axis must be 2^a 3^b 5^c with 5 <= K <= 64; a larger
  * grid returns NXM_ERR_CAPACITY.  It calls no cudaMalloc, cudaFree or other
  * allocating routine and copies nothing between host and device.

@@ -26,7 +26,7 @@ PROBE_LIB = os.path.join(ROOT, "libnxm_probe.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["k_neighbor.cu", "k_pairs.cu", "k_bonded.cu", "k_nonbonded.cu", "k_fft.cu", "k_pme.cu",
                 "k_integrate.cu", "nxm_engine.cu", "nxm_abi.cpp", "nxm_dispatcher.cpp", "k_pme_noalloc.cu",
-                "nxm_report.cpp"]
+                "nxm_report.cpp", "k_exclusions_build.cu"]
 HOST_SOURCES = ["nxm_xml.cpp", "nxm_io.cpp"]
 
 

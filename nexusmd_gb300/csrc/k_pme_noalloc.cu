@@ -12,7 +12,7 @@
 // :51-461) allocates its grids per evaluation.
 //
 // Limits: each grid axis K in [5, 64] with K = 2^a 3^b 5^c; any atom count.
-// Scratch: about 4.8 MB of device memory per device, for the lifetime of
+// Scratch: about 3.7 MB of device memory per device, for the lifetime of
 // the library.
 //
 // Set-up: the first call on a device (the device current at the call) looks
@@ -62,7 +62,7 @@ constexpr size_t kOffMod = kOffTw + align256(sizeof(float2) * 3 * kStaticMaxK); 
 constexpr size_t kOffAcc = kOffMod + align256(sizeof(double) * 3 * kStaticMaxK);
 constexpr size_t kGridPts = (size_t)kStaticMaxK * kStaticMaxK * kStaticMaxK;
 constexpr size_t kSpecPts = (size_t)kStaticMaxK * kStaticMaxK * kStaticMaxKh;
-constexpr size_t kOffReal = kOffAcc + align256(sizeof(long long) * kGridPts);
+constexpr size_t kOffReal = kOffAcc + align256(sizeof(int) * kGridPts);
 constexpr size_t kOffCplx = kOffReal + align256(sizeof(float) * kGridPts);
 constexpr size_t kOffEterm = kOffCplx + align256(sizeof(float2) * kSpecPts);
 constexpr size_t kScratchBytes = kOffEterm + align256(sizeof(float) * kSpecPts);
@@ -126,7 +126,7 @@ __device__ __forceinline__ void grid_coord(double p, double invL, int K, int &id
 // below 1e-7 (NonbondedForce.cpp:75-142).
 __global__ void k_noalloc_setup(unsigned char *scr, FftSysDev F, int nz, int ny, int nx) {
     __shared__ double s_mod[3][kStaticMaxK];
-    long long *acc = region<long long>(scr, kOffAcc);
+    int *acc = region<int>(scr, kOffAcc);
     long long npts = (long long)F.K[0] * F.K[1] * F.K[2];
     long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     long long nthr = (long long)gridDim.x * blockDim.x;
@@ -216,7 +216,8 @@ __global__ void k_noalloc_eterm(unsigned char *scr, Geometry g) {
     }
 }
 
-// ---- spread: one thread per atom, int64 fixed-point grid (2^-32 units).
+// ---- spread: one thread per atom, int32 fixed-point grid (2^-24 e units,
+// the grid word the FFT's first pass reads).
 __global__ void __launch_bounds__(128) k_noalloc_spread(unsigned char *scr, Geometry g, const double *xyz,
                                                         const double *charge, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -229,7 +230,7 @@ __global__ void __launch_bounds__(128) k_noalloc_spread(unsigned char *scr, Geom
         spline5(fr[d], th[d], dth[d]);
     }
     float q = (float)charge[i];
-    long long *acc = region<long long>(scr, kOffAcc);
+    int *acc = region<int>(scr, kOffAcc);
     int K0 = g.K[0], K1 = g.K[1], K2 = g.K[2];
     for (int ix = 0; ix < 5; ++ix) {
         int xi = idx[0] + ix;
@@ -244,8 +245,7 @@ __global__ void __launch_bounds__(128) k_noalloc_spread(unsigned char *scr, Geom
             for (int iz = 0; iz < 5; ++iz) {
                 int zi = idx[2] + iz;
                 zi -= zi >= K2 ? K2 : 0;
-                atomicAdd(reinterpret_cast<unsigned long long *>(acc + row + zi),
-                          static_cast<unsigned long long>(__float2ll_rn(qxy * th[2][iz] * 4294967296.0f)));
+                atomicAdd(acc + row + zi, __float2int_rn(qxy * th[2][iz] * 16777216.0f));
             }
         }
     }

@@ -48,6 +48,42 @@ __global__ void k_decide_graph(DevView v, cudaGraphConditionalHandle h) {
     cudaGraphSetConditional(h, rb ? 1u : 0u);
 }
 
+// Context creation: positions given per atom as (x, y, z) into x, y, z;
+// 1/m (0 for a massless particle, VerletIntegration.cpp:37-45; the division
+// rounds as the host's); slot = original index until the first sort.
+__global__ void k_init_atoms(DevView v, const double *xyz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.N) return;
+    v.x[i] = xyz[3 * (size_t)i];
+    v.y[i] = xyz[3 * (size_t)i + 1];
+    v.z[i] = xyz[3 * (size_t)i + 2];
+    const double m = v.mass[i];
+    v.invm[i] = m == 0.0 ? 0.0 : 1.0 / m;
+    v.orig[i] = i;
+    v.slot_of[i] = i;
+}
+
+static void launch_init_atoms(const DevView &v, const double *xyz, cudaStream_t st) {
+    if (v.N > 0) k_init_atoms<<<(v.N + 255) / 256, 256, 0, st>>>(v, xyz);
+}
+
+// A state vector given per original atom as (x, y, z) into slot order.
+__global__ void k_state_to_slots(DevView v, const double *xyz, double *dx, double *dy, double *dz) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= v.N) return;
+    const size_t o = 3 * (size_t)v.orig[s];
+    dx[s] = xyz[o];
+    dy[s] = xyz[o + 1];
+    dz[s] = xyz[o + 2];
+}
+
+// FP32 copies of the bonded parameters (each double rounded once, as the
+// FP64 terms' values).
+__global__ void k_params_f32(const double2 *a, float2 *b, int n) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) b[k] = make_float2((float)a[k].x, (float)a[k].y);
+}
+
 // ------------------------------------------------------------ host maths
 
 static bool smooth235(int n) {
@@ -394,30 +430,6 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     double skin = opt.skin > 0 ? opt.skin : 0.0;
     int stride = 0, hood_cap = 0;
     std::vector<int> group_g(S, 1);
-    // The exclusion sets (a host-side breadth-first search per atom) do not
-    // depend on anything the device set-up below needs, so they are built on
-    // a second host thread while the device memory is allocated and filled;
-    // the thread is joined before their first use.
-    std::string ex_err;
-    struct Joiner {
-        std::thread t;
-        ~Joiner() {
-            if (t.joinable()) t.join();
-        }
-    } ex_job;
-    ex_job.t = std::thread([this, &systems, &eoff, &elst, &ex_pairs, &ex_err] {
-        const double t0 = now_ms();
-        int o = 0;
-        for (const HostSystem &h : systems) {
-            std::string e = exclusion_rows(h, o, eoff, elst, ex_pairs);
-            if (!e.empty()) {
-                ex_err = e;
-                break;
-            }
-            o += h.n;
-        }
-        create_ms_[8] = now_ms() - t0;
-    });
     for (int s = 0; s < S; ++s) {
         const HostSystem &h = systems[s];
         SysDev &D = sysd_[s];
@@ -573,7 +585,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     v_.mixed = mixed_;
     v_.stride = stride;
     SysDev *dsys = dalloc<SysDev>(S);
-    cudaMemcpy(dsys, sysd_.data(), sizeof(SysDev) * S, cudaMemcpyHostToDevice);
+    cudaMemcpyAsync(dsys, sysd_.data(), sizeof(SysDev) * S, cudaMemcpyHostToDevice, st_);
     v_.sys = dsys;
     v_.sys_of = dalloc<int>(N_);
     v_.orig = dalloc<int>(N_);
@@ -624,7 +636,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         v_.groups = dalloc<CellGroup>(gr.size());
         v_.gspan = dalloc<int>(gr.size() * (size_t)kGroupSpanWords);
         v_.gspan_n = dalloc<int2>(gr.size());
-        cudaMemcpy(v_.groups, gr.data(), sizeof(CellGroup) * gr.size(), cudaMemcpyHostToDevice);
+        cudaMemcpyAsync(v_.groups, gr.data(), sizeof(CellGroup) * gr.size(), cudaMemcpyHostToDevice, st_);
     }
     tiles_set_smem(hood_cap);
     v_.ncount = dalloc<int>(N_);
@@ -634,43 +646,46 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     v_.tmp = dalloc<double>(11 * (size_t)N_);
     if (!v_.nl16 || !v_.tmp) return "device allocation failed (neighbour list)";
 
-    // host staging in original order (slot = original index until the first sort)
-    std::vector<int> sys_of(N_), iota(N_);
-    std::vector<double> hx(N_), hy(N_), hz(N_), hm(N_), him(N_), hq(N_), hs(N_), he(N_);
+    // per-atom inputs in original order (slot = original index until the
+    // first sort): each array from the caller's in one copy (a batch's
+    // systems concatenated), the positions as given (x, y, z per atom) into
+    // scratch, split and 1/m formed on the device (k_init_atoms)
+    // uploads in the stream's order (the kernels of the set-up follow them
+    // there); from pageable memory the call returns once the source is
+    // consumed
+    auto up = [&](void *dst, const void *src, size_t bytes) {
+        const double t0 = now_ms();
+        cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st_);
+        create_ms_[7] += now_ms() - t0;
+    };
+    std::vector<int> sys_of(N_);
     {
         int o = 0;
         for (int s = 0; s < S; ++s) {
-            const HostSystem &h = systems[s];
-            for (int i = 0; i < h.n; ++i, ++o) {
-                sys_of[o] = s;
-                iota[o] = o;
-                hx[o] = positions[3 * (size_t)o];
-                hy[o] = positions[3 * (size_t)o + 1];
-                hz[o] = positions[3 * (size_t)o + 2];
-                hm[o] = h.mass[i];
-                him[o] = (h.mass[i] == 0.0) ? 0.0 : 1.0 / h.mass[i];  // VerletIntegration.cpp:37-45
-                hq[o] = h.q[i];
-                hs[o] = h.sig[i];
-                he[o] = h.eps[i];
-            }
+            std::fill(sys_of.begin() + o, sys_of.begin() + o + systems[s].n, s);
+            o += systems[s].n;
         }
     }
-    auto up = [&](void *dst, const void *src, size_t bytes) {
-        const double t0 = now_ms();
-        cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
-        create_ms_[7] += now_ms() - t0;
-    };
     up(v_.sys_of, sys_of.data(), sizeof(int) * N_);
-    up(v_.orig, iota.data(), sizeof(int) * N_);
-    up(v_.slot_of, iota.data(), sizeof(int) * N_);
-    up(v_.x, hx.data(), sizeof(double) * N_);
-    up(v_.y, hy.data(), sizeof(double) * N_);
-    up(v_.z, hz.data(), sizeof(double) * N_);
-    up(v_.mass, hm.data(), sizeof(double) * N_);
-    up(v_.invm, him.data(), sizeof(double) * N_);
-    up(v_.q, hq.data(), sizeof(double) * N_);
-    up(v_.sig, hs.data(), sizeof(double) * N_);
-    up(v_.eps, he.data(), sizeof(double) * N_);
+    {
+        std::vector<double> cat;
+        auto atoms = [&](double *dst, const std::vector<double> HostSystem::*field) {
+            const double *src = (systems[0].*field).data();
+            if (S > 1) {
+                cat.clear();
+                cat.reserve(N_);
+                for (const HostSystem &h : systems) cat.insert(cat.end(), (h.*field).begin(), (h.*field).end());
+                src = cat.data();
+            }
+            up(dst, src, sizeof(double) * N_);
+        };
+        atoms(v_.mass, &HostSystem::mass);
+        atoms(v_.q, &HostSystem::q);
+        atoms(v_.sig, &HostSystem::sig);
+        atoms(v_.eps, &HostSystem::eps);
+    }
+    up(v_.tmp, positions, sizeof(double) * 3 * (size_t)N_);
+    launch_init_atoms(v_, v_.tmp, st_);
 
     // cell-image displacement table: code ((ox+2)*5 + (oy+2))*12 + (oz+2) -> -(o . cs),
     // o relative to the first cell of a group (oz from -2 to kMaxGroupCells + 1)
@@ -704,44 +719,149 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         up(v_.cgrid, cg.data(), sizeof(float2) * cg.size());
     }
 
-    // exclusion CSR (batch-global original indices), from the host thread
-    ex_job.t.join();
-    if (!ex_err.empty()) return ex_err;
-    v_.excl_off = dalloc<int>(N_ + 1);
-    v_.excl_lst = dalloc<int>(elst.size());
-    up(v_.excl_off, eoff.data(), sizeof(int) * (N_ + 1));
-    if (!elst.empty()) up(v_.excl_lst, elst.data(), sizeof(int) * elst.size());
+    // exclusion CSR (batch-global original indices) and the excluded pairs
+    // j > i of the systems with the nonbonded force, built on the device
+    // (k_exclusions_build.cu); a row too long for it: built on the host
+    bool ex_on_host = false;
+    {
+        const double t0 = now_ms();
+        std::vector<int2> eb;  // every bond, batch-global (the search ignores the force mask)
+        std::vector<int> depth(S), nb_on(S);
+        {
+            size_t nbt = 0;
+            for (const HostSystem &h : systems) nbt += h.bonds.size() / 2;
+            eb.reserve(nbt);
+            int o = 0;
+            for (int s = 0; s < S; ++s) {
+                const HostSystem &h = systems[s];
+                for (size_t b = 0; b < h.bonds.size() / 2; ++b) {
+                    const int i = h.bonds[2 * b], j = h.bonds[2 * b + 1];
+                    if (i < 0 || j < 0 || i >= h.n || j >= h.n)
+                        return "createExclusions: Illegal particle index in list of bonds";
+                    eb.push_back(make_int2(o + i, o + j));
+                }
+                depth[s] = h.excl_depth;
+                nb_on[s] = (h.force_mask & NXM_FORCE_NONBONDED) ? 1 : 0;
+                o += h.n;
+            }
+        }
+        v_.nxc = (int)xc_pairs.size();
+        v_.xc_orig = dalloc<int2>(v_.nxc);
+        if (v_.nxc) up(v_.xc_orig, xc_pairs.data(), sizeof(int2) * v_.nxc);
+        ExclBuild B{};
+        B.n = N_;
+        B.nb = (int)eb.size();
+        B.nx = v_.nxc;
+        int2 *dbonds = dalloc<int2>(std::max<size_t>(eb.size(), 1));
+        if (!eb.empty()) up(dbonds, eb.data(), sizeof(int2) * eb.size());
+        B.bonds = dbonds;
+        B.xc = v_.xc_orig;
+        B.sys_of = v_.sys_of;
+        int *tabs = dalloc<int>(2 * (size_t)S);
+        up(tabs, depth.data(), sizeof(int) * S);
+        up(tabs + S, nb_on.data(), sizeof(int) * S);
+        B.depth = tabs;
+        B.nb_on = tabs + S;
+        int *w4 = dalloc<int>(4 * (size_t)N_);
+        B.deg = w4;
+        B.xdeg = w4 + N_;
+        B.afill = w4 + 2 * (size_t)N_;
+        B.xfill = w4 + 3 * (size_t)N_;
+        B.aoff = dalloc<int>(N_ + 1);
+        B.xoff = dalloc<int>(N_ + 1);
+        B.adj = dalloc<int>(std::max<size_t>(2 * eb.size(), 1));
+        B.xadj = dalloc<int>(std::max<size_t>(2 * xc_pairs.size(), 1));
+        B.len = dalloc<int>(N_);
+        B.plen = dalloc<int>(N_);
+        B.eoff = dalloc<int>(N_ + 1);
+        B.poff = dalloc<int>(N_ + 1);
+        B.overflow = dalloc<int>(1);
+        if (alloc_failed_) return "device allocation failed (exclusions)";
+        cudaMemsetAsync(B.overflow, 0, sizeof(int), st_);
+        launch_exclusions_count(B, st_);
+        int tail[3] = {0, 0, 0};
+        cudaMemcpyAsync(tail, B.eoff + N_, sizeof(int), cudaMemcpyDeviceToHost, st_);
+        cudaMemcpyAsync(tail + 1, B.poff + N_, sizeof(int), cudaMemcpyDeviceToHost, st_);
+        cudaMemcpyAsync(tail + 2, B.overflow, sizeof(int), cudaMemcpyDeviceToHost, st_);
+        cudaStreamSynchronize(st_);
+        std::string e = check("exclusions");
+        if (!e.empty()) return e;
+        if (tail[2]) {
+            ex_on_host = true;
+            int o = 0;
+            for (const HostSystem &h : systems) {
+                e = exclusion_rows(h, o, eoff, elst, ex_pairs);
+                if (!e.empty()) return e;
+                o += h.n;
+            }
+            v_.excl_off = dalloc<int>(N_ + 1);
+            v_.excl_lst = dalloc<int>(std::max<size_t>(elst.size(), 1));
+            up(v_.excl_off, eoff.data(), sizeof(int) * (N_ + 1));
+            if (!elst.empty()) up(v_.excl_lst, elst.data(), sizeof(int) * elst.size());
+        } else {
+            v_.excl_off = B.eoff;
+            v_.excl_lst = dalloc<int>(std::max(tail[0], 1));
+            v_.nex = tail[1];
+            v_.ex_orig = dalloc<int2>(std::max(v_.nex, 1));
+            if (alloc_failed_) return "device allocation failed (exclusions)";
+            launch_exclusions_fill(B, v_.excl_lst, v_.ex_orig, st_);
+        }
+        create_ms_[8] = now_ms() - t0;
+    }
 
-    // terms (batch-global original indices); kinds disabled by the force mask get a zero count
+    // terms (batch-global original indices); kinds disabled by the force mask
+    // get a zero count.  Sized once, parameters copied as given.
     std::vector<int2> bo;
     std::vector<double2> bp, ap, tp;
     std::vector<int4> ao, to;
     std::vector<int> tper;
     {
+        size_t nb = 0, na = 0, nt = 0;
+        for (const HostSystem &h : systems) {
+            if (h.force_mask & NXM_FORCE_BOND) nb += h.bonds.size() / 2;
+            if (h.force_mask & NXM_FORCE_ANGLE) na += h.angles.size() / 3;
+            if (h.force_mask & NXM_FORCE_TORSION) nt += h.torsions.size() / 4;
+        }
+        bo.resize(nb);
+        bp.resize(nb);
+        ao.resize(na);
+        ap.resize(na);
+        to.resize(nt);
+        tp.resize(nt);
+        tper.resize(nt);
+        size_t kb = 0, ka = 0, kt = 0;
         int o = 0;
-        for (int s = 0; s < S; ++s) {
-            const HostSystem &h = systems[s];
-            if (h.force_mask & NXM_FORCE_BOND)
-                for (size_t b = 0; b < h.bonds.size() / 2; ++b) {
-                    bo.push_back(make_int2(o + h.bonds[2 * b], o + h.bonds[2 * b + 1]));
-                    bp.push_back(make_double2(h.bprm[2 * b], h.bprm[2 * b + 1]));
+        for (const HostSystem &h : systems) {
+            for (int a : h.angles)
+                if (a < 0 || a >= h.n) return "angle atom index out of range";
+            for (int a : h.torsions)
+                if (a < 0 || a >= h.n) return "torsion atom index out of range";
+            if (h.force_mask & NXM_FORCE_BOND) {
+                const size_t m = h.bonds.size() / 2;
+                const int *b = h.bonds.data();
+                for (size_t k = 0; k < m; ++k) bo[kb + k] = make_int2(o + b[2 * k], o + b[2 * k + 1]);
+                if (m) std::memcpy(&bp[kb], h.bprm.data(), sizeof(double2) * m);
+                kb += m;
+            }
+            if (h.force_mask & NXM_FORCE_ANGLE) {
+                const size_t m = h.angles.size() / 3;
+                const int *a = h.angles.data();
+                for (size_t k = 0; k < m; ++k)
+                    ao[ka + k] = make_int4(o + a[3 * k], o + a[3 * k + 1], o + a[3 * k + 2], 0);
+                if (m) std::memcpy(&ap[ka], h.aprm.data(), sizeof(double2) * m);
+                ka += m;
+            }
+            if (h.force_mask & NXM_FORCE_TORSION) {
+                const size_t m = h.torsions.size() / 4;
+                const int *t = h.torsions.data();
+                for (size_t k = 0; k < m; ++k)
+                    to[kt + k] = make_int4(o + t[4 * k], o + t[4 * k + 1], o + t[4 * k + 2], o + t[4 * k + 3]);
+                if (m) {
+                    std::memcpy(&tp[kt], h.tprm.data(), sizeof(double2) * m);
+                    std::memcpy(&tper[kt], h.tper.data(), sizeof(int) * m);
                 }
-            if (h.force_mask & NXM_FORCE_ANGLE)
-                for (size_t a = 0; a < h.angles.size() / 3; ++a) {
-                    ao.push_back(make_int4(o + h.angles[3 * a], o + h.angles[3 * a + 1], o + h.angles[3 * a + 2], 0));
-                    ap.push_back(make_double2(h.aprm[2 * a], h.aprm[2 * a + 1]));
-                }
-            if (h.force_mask & NXM_FORCE_TORSION)
-                for (size_t t = 0; t < h.torsions.size() / 4; ++t) {
-                    to.push_back(make_int4(o + h.torsions[4 * t], o + h.torsions[4 * t + 1], o + h.torsions[4 * t + 2],
-                                           o + h.torsions[4 * t + 3]));
-                    tp.push_back(make_double2(h.tprm[2 * t], h.tprm[2 * t + 1]));
-                    tper.push_back(h.tper[t]);
-                }
-            for (size_t k = 0; k < h.angles.size(); ++k)
-                if (h.angles[k] < 0 || h.angles[k] >= h.n) return "angle atom index out of range";
-            for (size_t k = 0; k < h.torsions.size(); ++k)
-                if (h.torsions[k] < 0 || h.torsions[k] >= h.n) return "torsion atom index out of range";
+                kt += m;
+            }
             o += h.n;
         }
     }
@@ -774,38 +894,31 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     if (mixed_) {
         // the FP32 engine's parameters rounded once here rather than in
         // every evaluation (the same values: the kernels round the same doubles)
-        auto f2 = [](const std::vector<double2> &a) {
-            std::vector<float2> o(a.size());
-            for (size_t k = 0; k < a.size(); ++k) o[k] = make_float2((float)a[k].x, (float)a[k].y);
-            return o;
-        };
-        std::vector<float2> bf = f2(bp), af = f2(ap), tf = f2(tp);
         v_.bond_prmf = dalloc<float2>(v_.nb);
         v_.angle_prmf = dalloc<float2>(v_.na);
         v_.tors_prmf = dalloc<float2>(v_.nt);
-        if (v_.nb) up(v_.bond_prmf, bf.data(), sizeof(float2) * v_.nb);
-        if (v_.na) up(v_.angle_prmf, af.data(), sizeof(float2) * v_.na);
-        if (v_.nt) up(v_.tors_prmf, tf.data(), sizeof(float2) * v_.nt);
+        if (alloc_failed_) return "device allocation failed (terms)";
+        const std::pair<const double2 *, float2 *> pr[3] = {
+            {v_.bond_prm, v_.bond_prmf}, {v_.angle_prm, v_.angle_prmf}, {v_.tors_prm, v_.tors_prmf}};
+        const int cnt[3] = {v_.nb, v_.na, v_.nt};
+        for (int k = 0; k < 3; ++k)
+            if (cnt[k]) k_params_f32<<<(cnt[k] + 255) / 256, 256, 0, st_>>>(pr[k].first, pr[k].second, cnt[k]);
     }
-    // exclusion correction pairs: only for systems with nonbonded enabled
-    {
+    // exclusion correction pairs (host-built sets): only for systems with
+    // nonbonded enabled
+    if (ex_on_host) {
         std::vector<int2> keep;
         for (auto &e : ex_pairs)
             if (sysh_[sys_of[e.x]].force_mask & NXM_FORCE_NONBONDED) keep.push_back(e);
         ex_pairs.swap(keep);
+        v_.nex = (int)ex_pairs.size();
+        v_.ex_orig = dalloc<int2>(v_.nex);
+        if (v_.nex) up(v_.ex_orig, ex_pairs.data(), sizeof(int2) * v_.nex);
     }
-    v_.nex = (int)ex_pairs.size();
-    v_.ex_orig = dalloc<int2>(v_.nex);
     v_.ex_slot = dalloc<int2>(v_.nex);
-    if (v_.nex) up(v_.ex_orig, ex_pairs.data(), sizeof(int2) * v_.nex);
-    v_.nxc = (int)xc_pairs.size();
-    v_.xc_orig = dalloc<int2>(v_.nxc);
     v_.xc_slot = dalloc<int2>(v_.nxc);
     v_.xc_prm = dalloc<double4>(v_.nxc);
-    if (v_.nxc) {
-        up(v_.xc_orig, xc_pairs.data(), sizeof(int2) * v_.nxc);
-        up(v_.xc_prm, xc_prm.data(), sizeof(double4) * v_.nxc);
-    }
+    if (v_.nxc) up(v_.xc_prm, xc_prm.data(), sizeof(double4) * v_.nxc);
     if (mixed_) {
         std::vector<float4> xf(xc_prm.size());
         for (size_t k = 0; k < xc_prm.size(); ++k)
@@ -1065,19 +1178,8 @@ std::string Engine::autotune() {
 std::string Engine::set_positions(const double *xyz) {
     // positions arrive in original order; the slot order is re-derived
     // from them by the forced rebuild of the next evaluation
-    std::vector<double> h(3 * (size_t)N_);
-    std::vector<int> orig(N_);
-    cudaMemcpy(orig.data(), v_.orig, sizeof(int) * N_, cudaMemcpyDeviceToHost);
-    std::vector<double> hx(N_), hy(N_), hz(N_);
-    for (int s = 0; s < N_; ++s) {
-        int o = orig[s];
-        hx[s] = xyz[3 * (size_t)o];
-        hy[s] = xyz[3 * (size_t)o + 1];
-        hz[s] = xyz[3 * (size_t)o + 2];
-    }
-    cudaMemcpy(v_.x, hx.data(), sizeof(double) * N_, cudaMemcpyHostToDevice);
-    cudaMemcpy(v_.y, hy.data(), sizeof(double) * N_, cudaMemcpyHostToDevice);
-    cudaMemcpy(v_.z, hz.data(), sizeof(double) * N_, cudaMemcpyHostToDevice);
+    cudaMemcpyAsync(v_.tmp, xyz, sizeof(double) * 3 * (size_t)N_, cudaMemcpyHostToDevice, st_);
+    if (N_ > 0) k_state_to_slots<<<(N_ + 255) / 256, 256, 0, st_>>>(v_, v_.tmp, v_.x, v_.y, v_.z);
     launch_derive_inputs(v_, st_);
     force_rebuild_ = true;
     cudaStreamSynchronize(st_);
@@ -1085,18 +1187,9 @@ std::string Engine::set_positions(const double *xyz) {
 }
 
 std::string Engine::set_velocities(const double *xyz) {
-    std::vector<int> orig(N_);
-    cudaMemcpy(orig.data(), v_.orig, sizeof(int) * N_, cudaMemcpyDeviceToHost);
-    std::vector<double> hx(N_), hy(N_), hz(N_);
-    for (int s = 0; s < N_; ++s) {
-        int o = orig[s];
-        hx[s] = xyz[3 * (size_t)o];
-        hy[s] = xyz[3 * (size_t)o + 1];
-        hz[s] = xyz[3 * (size_t)o + 2];
-    }
-    cudaMemcpy(v_.vx, hx.data(), sizeof(double) * N_, cudaMemcpyHostToDevice);
-    cudaMemcpy(v_.vy, hy.data(), sizeof(double) * N_, cudaMemcpyHostToDevice);
-    cudaMemcpy(v_.vz, hz.data(), sizeof(double) * N_, cudaMemcpyHostToDevice);
+    cudaMemcpyAsync(v_.tmp, xyz, sizeof(double) * 3 * (size_t)N_, cudaMemcpyHostToDevice, st_);
+    if (N_ > 0) k_state_to_slots<<<(N_ + 255) / 256, 256, 0, st_>>>(v_, v_.tmp, v_.vx, v_.vy, v_.vz);
+    cudaStreamSynchronize(st_);
     return check("set_velocities");
 }
 

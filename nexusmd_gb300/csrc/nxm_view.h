@@ -91,6 +91,21 @@ struct DevView {
     double skin_half2;   // (skin/2)^2; 0 disables the displacement check
 };
 
+// Context creation: the exclusion sets built on the device
+// (k_exclusions_build.cu).  deg, xdeg, afill and xfill are consecutive runs
+// of n ints (cleared by one memset).
+struct ExclBuild {
+    int n, nb, nx;               // atoms, bonds, exception pairs
+    const int2 *bonds, *xc;      // batch-global atom indices
+    const int *sys_of, *depth, *nb_on;
+    int *deg, *xdeg, *afill, *xfill;
+    int *aoff, *xoff, *adj, *xadj;
+    int *len, *plen, *eoff, *poff;
+    int *overflow;               // set when a row exceeds the device search's capacity
+};
+void launch_exclusions_count(const ExclBuild &b, cudaStream_t st);
+void launch_exclusions_fill(const ExclBuild &b, int *elst, int2 *pairs, cudaStream_t st);
+
 // kernel launchers (one per .cu file group)
 void launch_nlist_rebuild(const DevView &v, cudaStream_t st);
 void launch_build(const DevView &v, cudaStream_t st);

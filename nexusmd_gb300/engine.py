@@ -323,7 +323,7 @@ class Engine:
         return q, e, r
 
     CREATE_PHASES = ("host_setup", "device_alloc_upload", "pme_tables_fft_plan", "autotune", "graph_builds",
-                     "create_total", "of_which_alloc", "of_which_upload", "exclusions_thread")
+                     "create_total", "of_which_alloc", "of_which_upload", "of_which_exclusions")
 
     def create_timing(self):
         """Host milliseconds of context creation by phase, and whether the

@@ -201,11 +201,14 @@ def test_sparse_system_empty_cells(oracle):
         eng.close()
 
 
-@pytest.mark.parametrize("depth", [3, 2])
+@pytest.mark.parametrize("depth", [3, 2, 60])
 def test_exceptions_physics_mode(oracle, depth):
     """Scaled 1-4 exceptions (OpenMM semantics) vs the oracle.  With depth 2
     the 1-4 pairs are excluded only because they are exceptions, so the
-    engine's union of bonded exclusions and exception pairs is exercised."""
+    engine's union of bonded exclusions and exception pairs is exercised.
+    The exclusion sets are built on the device; with depth 60 the chain
+    atoms' sets (well over 96 atoms) exceed the device search and the host
+    builds them instead."""
     s = sy.with_exceptions(sy.config_system(1))
     lb, ub = np.zeros(3), s.box.copy()
     box = oracle.box_explicit(lb, ub)
