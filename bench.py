@@ -666,6 +666,13 @@ def native(args):
         # the same end-to-end measurement over 1,000 steps
         t_long, _ = e2e_run(s, v0, kw, 1000)
         out["e2e"]["value_1000_steps"] = sig(s.n * 1000 / t_long)
+        # and the device-timed throughput of the same 1,000 steps from the
+        # same start (a fresh context, its first step the forced list build)
+        eng_l = Engine(s, precision=1, **kw)
+        eng_l.set_velocities(v0)
+        ms_l = eng_l.time_steps(1000, DT_PS)
+        eng_l.close()
+        out["e2e"]["device_value_1000_steps"] = sig(s.n * 1000 / (ms_l * 1e-3))
         # plain FP64 form of the same engine
         eng64 = Engine(s, precision=0, **kw)
         eng64.set_velocities(v0)

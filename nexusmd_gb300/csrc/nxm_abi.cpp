@@ -69,22 +69,23 @@ int nxm_create(const nxm_system_desc *systems, int32_t n_systems, const nxm_opti
             return fail(NXM_ERR_INVALID, "nxm_create: term count without arrays");
         int n = d.n_atoms;
         h.n = n;
-        h.mass.assign(d.masses, d.masses + n);
-        h.q.assign(d.charges, d.charges + n);
-        h.sig.assign(d.sigmas, d.sigmas + n);
-        h.eps.assign(d.epsilons, d.epsilons + n);
+        // the caller's arrays, read in place during the creation
+        h.mass = {d.masses, (size_t)n};
+        h.q = {d.charges, (size_t)n};
+        h.sig = {d.sigmas, (size_t)n};
+        h.eps = {d.epsilons, (size_t)n};
         if (d.n_bonds > 0) {
-            h.bonds.assign(d.bond_atoms, d.bond_atoms + 2 * (size_t)d.n_bonds);
-            h.bprm.assign(d.bond_params, d.bond_params + 2 * (size_t)d.n_bonds);
+            h.bonds = {d.bond_atoms, 2 * (size_t)d.n_bonds};
+            h.bprm = {d.bond_params, 2 * (size_t)d.n_bonds};
         }
         if (d.n_angles > 0) {
-            h.angles.assign(d.angle_atoms, d.angle_atoms + 3 * (size_t)d.n_angles);
-            h.aprm.assign(d.angle_params, d.angle_params + 2 * (size_t)d.n_angles);
+            h.angles = {d.angle_atoms, 3 * (size_t)d.n_angles};
+            h.aprm = {d.angle_params, 2 * (size_t)d.n_angles};
         }
         if (d.n_torsions > 0) {
-            h.torsions.assign(d.torsion_atoms, d.torsion_atoms + 4 * (size_t)d.n_torsions);
-            h.tprm.assign(d.torsion_params, d.torsion_params + 2 * (size_t)d.n_torsions);
-            h.tper.assign(d.torsion_periodicity, d.torsion_periodicity + d.n_torsions);
+            h.torsions = {d.torsion_atoms, 4 * (size_t)d.n_torsions};
+            h.tprm = {d.torsion_params, 2 * (size_t)d.n_torsions};
+            h.tper = {d.torsion_periodicity, (size_t)d.n_torsions};
         }
         h.cutoff = d.cutoff;
         h.tol = d.ewald_tolerance;
@@ -101,8 +102,8 @@ int nxm_create(const nxm_system_desc *systems, int32_t n_systems, const nxm_opti
         if (d.n_exceptions < 0 || (d.n_exceptions > 0 && (!d.exception_atoms || !d.exception_params)))
             return fail(NXM_ERR_INVALID, "nxm_create: exception count without arrays");
         if (d.n_exceptions > 0) {
-            h.exc.assign(d.exception_atoms, d.exception_atoms + 2 * (size_t)d.n_exceptions);
-            h.exc_prm.assign(d.exception_params, d.exception_params + 3 * (size_t)d.n_exceptions);
+            h.exc = {d.exception_atoms, 2 * (size_t)d.n_exceptions};
+            h.exc_prm = {d.exception_params, 3 * (size_t)d.n_exceptions};
         }
     }
     nxm_ctx *c = new (std::nothrow) nxm_ctx;

@@ -45,18 +45,17 @@ public:
         int n = (int)(ps.positions.size() / 3);
         nxm::HostSystem h;
         h.n = n;
-        h.mass = ps.masses;
-        h.mass.resize(n, 0.0);
-        h.q.assign(n, 0.0);
-        h.sig.assign(n, 0.0);
-        h.eps.assign(n, 0.0);
+        // the arrays the engine reads during its creation
+        std::vector<double> mass = ps.masses, q(n, 0.0), sig(n, 0.0), eps(n, 0.0), bprm, aprm, tprm, exc_prm;
+        std::vector<int> bonds, angles, torsions, tper, exc;
+        mass.resize(n, 0.0);
         if (nonbondedForceEnabled) {
             if ((int)ps.nb.particles.size() < n)
                 throw std::runtime_error("NonbondedForce has fewer particles than the state has positions");
             for (int i = 0; i < n; ++i) {
-                h.q[i] = ps.nb.particles[i].q;
-                h.sig[i] = ps.nb.particles[i].sig;
-                h.eps[i] = ps.nb.particles[i].eps;
+                q[i] = ps.nb.particles[i].q;
+                sig[i] = ps.nb.particles[i].sig;
+                eps[i] = ps.nb.particles[i].eps;
             }
             h.cutoff = ps.nb.cutoff;
             h.tol = ps.nb.ewaldTolerance;
@@ -64,21 +63,21 @@ public:
             h.sw_dist = ps.nb.switchingDistance;
         }
         for (auto &b : ps.bonds) {
-            h.bonds.push_back(b.p1);
-            h.bonds.push_back(b.p2);
-            h.bprm.push_back(b.d);
-            h.bprm.push_back(b.k);
+            bonds.push_back(b.p1);
+            bonds.push_back(b.p2);
+            bprm.push_back(b.d);
+            bprm.push_back(b.k);
         }
         for (auto &a : ps.angles) {
-            h.angles.insert(h.angles.end(), {a.p1, a.p2, a.p3});
-            h.aprm.push_back(a.a);
-            h.aprm.push_back(a.k);
+            angles.insert(angles.end(), {a.p1, a.p2, a.p3});
+            aprm.push_back(a.a);
+            aprm.push_back(a.k);
         }
         for (auto &t : ps.torsions) {
-            h.torsions.insert(h.torsions.end(), {t.p1, t.p2, t.p3, t.p4});
-            h.tprm.push_back(t.k);
-            h.tprm.push_back(t.phase);
-            h.tper.push_back(t.periodicity);
+            torsions.insert(torsions.end(), {t.p1, t.p2, t.p3, t.p4});
+            tprm.push_back(t.k);
+            tprm.push_back(t.phase);
+            tper.push_back(t.periodicity);
         }
         h.force_mask = (harmonicBondForceEnabled ? NXM_FORCE_BOND : 0) | (harmonicAngleForceEnabled ? NXM_FORCE_ANGLE : 0) |
                        (periodicTorsionForceEnabled ? NXM_FORCE_TORSION : 0) |
@@ -91,11 +90,24 @@ public:
         if (opt.exceptions && nonbondedForceEnabled) {
             // <Exceptions> of the system XML in OpenMM semantics (the reference ignores them)
             for (auto &x : ps.nb.exceptions) {
-                h.exc.push_back(x.p1);
-                h.exc.push_back(x.p2);
-                h.exc_prm.insert(h.exc_prm.end(), {x.q, x.sig, x.eps});
+                exc.push_back(x.p1);
+                exc.push_back(x.p2);
+                exc_prm.insert(exc_prm.end(), {x.q, x.sig, x.eps});
             }
         }
+        h.mass = mass;
+        h.q = q;
+        h.sig = sig;
+        h.eps = eps;
+        h.bonds = bonds;
+        h.bprm = bprm;
+        h.angles = angles;
+        h.aprm = aprm;
+        h.torsions = torsions;
+        h.tprm = tprm;
+        h.tper = tper;
+        h.exc = exc;
+        h.exc_prm = exc_prm;
         auto eng = std::make_unique<nxm::Engine>();
         std::string err = eng->init({h}, opt, ps.positions.data());
         if (!err.empty()) throw std::runtime_error(err);

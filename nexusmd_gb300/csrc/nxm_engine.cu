@@ -669,7 +669,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     up(v_.sys_of, sys_of.data(), sizeof(int) * N_);
     {
         std::vector<double> cat;
-        auto atoms = [&](double *dst, const std::vector<double> HostSystem::*field) {
+        auto atoms = [&](double *dst, const Span<double> HostSystem::*field) {
             const double *src = (systems[0].*field).data();
             if (S > 1) {
                 cat.clear();

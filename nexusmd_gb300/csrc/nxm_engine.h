@@ -15,11 +15,29 @@ constexpr int kProfilePhases = 8;
 constexpr int kLayoutWords = 11;
 constexpr int kCreatePhases = 9;
 
+// A read-only view of a caller's array (valid for the duration of the call
+// that receives it): context creation reads the inputs in place.
+template <class T>
+struct Span {
+    const T *p = nullptr;
+    size_t n = 0;
+    Span() = default;
+    Span(const T *ptr, size_t count) : p(ptr), n(count) {}
+    Span(const std::vector<T> &v) : p(v.data()), n(v.size()) {}  // NOLINT: views a vector the caller keeps
+    const T *data() const { return p; }
+    size_t size() const { return n; }
+    bool empty() const { return n == 0; }
+    const T &operator[](size_t i) const { return p[i]; }
+    const T *begin() const { return p; }
+    const T *end() const { return p + n; }
+};
+
+// One system's inputs to Engine::init, viewed in the caller's arrays.
 struct HostSystem {
     int n = 0;
-    std::vector<double> mass, q, sig, eps;
-    std::vector<int> bonds, angles, torsions, tper;  // flattened atom indices
-    std::vector<double> bprm, aprm, tprm;
+    Span<double> mass, q, sig, eps;
+    Span<int> bonds, angles, torsions, tper;  // flattened atom indices
+    Span<double> bprm, aprm, tprm;
     double cutoff = 1.0, tol = 5e-4;
     int use_switch = 0;
     double sw_dist = 0.0;
@@ -29,8 +47,8 @@ struct HostSystem {
     int force_mask = 15;
     int excl_depth = 3;
     // exception pairs (OpenMM semantics): atoms, and chargeProd / sigma / epsilon
-    std::vector<int> exc;
-    std::vector<double> exc_prm;
+    Span<int> exc;
+    Span<double> exc_prm;
 };
 
 struct SysHost {

@@ -201,8 +201,8 @@ class Engine:
         opt.device, opt.max_neighbors = int(device), int(max_neighbors)
         opt.fft_path, opt.autotune = int(fft_path), 1 if autotune else 0
         h = C.c_void_p()
-        _check(L.nxm_create(descs, len(systems), C.byref(opt), np.concatenate(pos), C.byref(h)),
-               "nxm_create")
+        xyz = pos[0] if len(pos) == 1 else np.concatenate(pos)
+        _check(L.nxm_create(descs, len(systems), C.byref(opt), xyz, C.byref(h)), "nxm_create")
         self._h = h
         self._L = L
         self.precision = precision
