@@ -128,59 +128,114 @@ __global__ void k_ex_fill(ExclInput in, const int *eoff, const int *poff, int *e
         if (row[k] > i) *pd++ = make_int2(i, row[k]);
 }
 
-// Exclusive scan of n ints by one block; out[n] = total.
-__global__ void k_ex_scan(const int *in, int *out, int n) {
+// Exclusive scan of n ints, out[n] = total: each block scans kScanTile
+// consecutive values (four per thread) and records its total, one block
+// scans the totals, and every block adds its offset.
+constexpr int kScanThreads = 1024, kScanTile = 4 * kScanThreads;
+
+// Exclusive scan of the block's values in place (v: this thread's value);
+// returns the block total to every thread.
+__device__ __forceinline__ int block_scan(int &v) {
     __shared__ int wsum[32];
-    __shared__ int carry;
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (threadIdx.x == 0) carry = 0;
+    int xs = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(full, xs, o);
+        if (lane >= o) xs += y;
+    }
+    if (lane == 31) wsum[w] = xs;
     __syncthreads();
-    for (int base = 0; base < n; base += blockDim.x) {
-        const int i = base + threadIdx.x;
-        const int val = i < n ? in[i] : 0;
-        int xs = val;
+    if (w == 0) {
+        int ws = lane < nw ? wsum[lane] : 0;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(full, xs, o);
-            if (lane >= o) xs += y;
+            const int y = __shfl_up_sync(full, ws, o);
+            if (lane >= o) ws += y;
         }
-        if (lane == 31) wsum[w] = xs;
-        __syncthreads();
-        if (w == 0) {
-            int ws = lane < nw ? wsum[lane] : 0;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int y = __shfl_up_sync(full, ws, o);
-                if (lane >= o) ws += y;
-            }
-            wsum[lane] = ws;
-        }
-        __syncthreads();
-        const int prefix = carry + (w > 0 ? wsum[w - 1] : 0) + xs - val;
-        if (i < n) out[i] = prefix;
-        __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry = prefix + val;
-        __syncthreads();
+        wsum[lane] = ws;
     }
-    if (threadIdx.x == 0) out[n] = carry;
+    __syncthreads();
+    const int total = wsum[nw - 1];
+    v = (w > 0 ? wsum[w - 1] : 0) + xs - v;
+    __syncthreads();  // wsum is reused by the next call
+    return total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_ex_scan_tiles(const int *in, int *out, int *tile_sum, int n) {
+    const int base = blockIdx.x * kScanTile + 4 * threadIdx.x;
+    int a[4], s = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        a[k] = base + k < n ? in[base + k] : 0;
+        s += a[k];
+    }
+    int pre = s;
+    const int total = block_scan(pre);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (base + k < n) out[base + k] = pre;
+        pre += a[k];
+    }
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+}
+
+// the tile totals (at most kScanTile of them, so one tile) and out[n]
+__global__ void __launch_bounds__(kScanThreads) k_ex_scan_sums(int *tile_sum, int ntiles, int *out, int n) {
+    const int base = 4 * threadIdx.x;
+    int a[4], s = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        a[k] = base + k < ntiles ? tile_sum[base + k] : 0;
+        s += a[k];
+    }
+    int pre = s;
+    const int total = block_scan(pre);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        if (base + k < ntiles) tile_sum[base + k] = pre;
+        pre += a[k];
+    }
+    if (threadIdx.x == 0) out[n] = total;
+}
+
+__global__ void k_ex_scan_add(int *out, const int *tile_sum, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] += tile_sum[i / kScanTile];
+}
+
+// Scan of n <= kScanTile^2 values (tile_sum holds n / kScanTile + 1 words).
+static void ex_scan(const int *in, int *out, int *tile_sum, int n, cudaStream_t st) {
+    const int ntiles = (n + kScanTile - 1) / kScanTile;
+    if (ntiles > 0) k_ex_scan_tiles<<<ntiles, kScanThreads, 0, st>>>(in, out, tile_sum, n);
+    k_ex_scan_sums<<<1, kScanThreads, 0, st>>>(tile_sum, ntiles, out, n);
+    if (ntiles > 1) k_ex_scan_add<<<(n + 255) / 256, 256, 0, st>>>(out, tile_sum, n);
 }
 
 static int nblocks(long long n, int t) { return (int)((n + t - 1) / t); }
 
+// A batch beyond the scans' reach (over 16.7 M atoms) reports overflow: the
+// host builds its sets.
+__global__ void k_ex_too_large(int *overflow) { *overflow = 1; }
+
 void launch_exclusions_count(const ExclBuild &b, cudaStream_t st) {
+    if ((long long)b.n > (long long)kScanTile * kScanTile) {
+        k_ex_too_large<<<1, 1, 0, st>>>(b.overflow);
+        return;
+    }
     const long long items = (long long)b.nb + b.nx;
     cudaMemsetAsync(b.deg, 0, sizeof(int) * 4 * (size_t)b.n, st);  // deg, xdeg, afill, xfill
     if (items > 0) k_ex_degree<<<nblocks(items, 256), 256, 0, st>>>(b.bonds, b.nb, b.xc, b.nx, b.deg, b.xdeg);
-    k_ex_scan<<<1, 1024, 0, st>>>(b.deg, b.aoff, b.n);
-    k_ex_scan<<<1, 1024, 0, st>>>(b.xdeg, b.xoff, b.n);
+    ex_scan(b.deg, b.aoff, b.tile_sum, b.n, st);
+    ex_scan(b.xdeg, b.xoff, b.tile_sum, b.n, st);
     if (items > 0)
         k_ex_adjacency<<<nblocks(items, 256), 256, 0, st>>>(b.bonds, b.nb, b.xc, b.nx, b.aoff, b.xoff, b.afill,
                                                              b.xfill, b.adj, b.xadj);
     const ExclInput in{b.sys_of, b.depth, b.nb_on, b.aoff, b.adj, b.xoff, b.xadj, b.n, b.overflow};
     if (b.n > 0) k_ex_count<<<nblocks(b.n, 128), 128, 0, st>>>(in, b.len, b.plen);
-    k_ex_scan<<<1, 1024, 0, st>>>(b.len, b.eoff, b.n);
-    k_ex_scan<<<1, 1024, 0, st>>>(b.plen, b.poff, b.n);
+    ex_scan(b.len, b.eoff, b.tile_sum, b.n, st);
+    ex_scan(b.plen, b.poff, b.tile_sum, b.n, st);
 }
 
 void launch_exclusions_fill(const ExclBuild &b, int *elst, int2 *pairs, cudaStream_t st) {

@@ -775,6 +775,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         B.plen = dalloc<int>(N_);
         B.eoff = dalloc<int>(N_ + 1);
         B.poff = dalloc<int>(N_ + 1);
+        B.tile_sum = dalloc<int>(N_ / 4096 + 2);
         B.overflow = dalloc<int>(1);
         if (alloc_failed_) return "device allocation failed (exclusions)";
         cudaMemsetAsync(B.overflow, 0, sizeof(int), st_);

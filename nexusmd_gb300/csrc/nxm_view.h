@@ -101,6 +101,7 @@ struct ExclBuild {
     int *deg, *xdeg, *afill, *xfill;
     int *aoff, *xoff, *adj, *xadj;
     int *len, *plen, *eoff, *poff;
+    int *tile_sum;               // scan scratch: n / 4096 + 1 words
     int *overflow;               // set when a row exceeds the device search's capacity
 };
 void launch_exclusions_count(const ExclBuild &b, cudaStream_t st);
