@@ -37,6 +37,7 @@ constexpr int kMaxExclFast = 32;
 // cell-image displacement table per system: 5 (x) * 5 (y) * 12 (z) codes
 constexpr int kDtabStride = 320;
 constexpr int kMaxGroupCells = 8;  // cells per group of the tile kernels (5*5*(8+4) = 300 codes)
+constexpr int kMaxGroupCellsWide = 4;  // the same with one 32-warp tile block per SM (FP32 tile extent)
 constexpr int kMaxSmemDevices = 64;  // devices whose shared-memory attributes are tracked
 
 // Energy slots per system.

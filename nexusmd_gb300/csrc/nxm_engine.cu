@@ -430,6 +430,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     double skin = opt.skin > 0 ? opt.skin : 0.0;
     int stride = 0, hood_cap = 0;
     std::vector<int> group_g(S, 1);
+    std::vector<double> cell_atoms_s(S, 0.0);  // mean atoms per cell
     for (int s = 0; s < S; ++s) {
         const HostSystem &h = systems[s];
         SysDev &D = sysd_[s];
@@ -565,7 +566,41 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         group_g[s] = G;
         int hood = (int)(25.0 * (G + 4) * cell_atoms * 1.25 + 128);
         hood_cap = std::max(hood_cap, hood);
+        cell_atoms_s[s] = cell_atoms;
         off += h.n;
+    }
+    if (hood_cap > 4400) {
+        // Some system's one-cell neighbourhood exceeds what two blocks per
+        // SM can stage, so the tile kernels run one block of 32 warps per SM
+        // (k_pairs.cu): then every system takes the longest groups, up to
+        // kMaxGroupCellsWide cells, whose neighbourhood stays within ~8,000
+        // atoms (one block's shared memory; 16-bit list entries address
+        // 8,191), split evenly along the column, up to the whole column --
+        // beyond nz - 4 a cell enters the neighbourhood twice, as two
+        // periodic images at least a box edge (> twice the list radius)
+        // apart, so at most one image of an atom is within the list radius,
+        // as in boxes of four cells.  A block's 32 warps then have 40-130
+        // atoms to take instead of 17-58, and each atom stages about half
+        // as many neighbours.  The cap keeps the tile's FP32 coordinates
+        // (relative to the group's first cell) within about six cells: at
+        // config 4 (32 systems) groups of up to 4 cells took the step 1.04
+        // -> 0.93 ms with the largest per-atom force error 0.077 kJ/mol/nm
+        // against the FP64 oracle; up to 5 or 8 cells, 0.89 / 0.86 ms but
+        // 0.35 kJ/mol/nm.
+        hood_cap = 0;
+        for (int s = 0; s < S; ++s) {
+            const int nz = sysd_[s].nc[2];
+            int G = 1;
+            for (int g = std::min(kMaxGroupCellsWide, nz); g >= 1; --g)
+                if (25.0 * (g + 4) * cell_atoms_s[s] * 1.25 + 128 <= 8000.0) {
+                    G = g;
+                    break;
+                }
+            const int ng = (nz + G - 1) / G;  // groups per column, of near-equal length
+            G = (nz + ng - 1) / ng;
+            group_g[s] = G;
+            hood_cap = std::max(hood_cap, (int)(25.0 * (G + 4) * cell_atoms_s[s] * 1.25 + 128));
+        }
     }
     group_g_ = group_g;
     if (opt.max_neighbors > 0) stride = opt.max_neighbors;

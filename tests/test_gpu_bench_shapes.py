@@ -8,8 +8,9 @@ pairs as exceptions scaled 0.8333/0.5, explicit periodic box):
 * a config-5-shaped system: config 5's density, composition, cutoff
   (1.2 nm), Ewald tolerance (1e-5) and PME grid (180^3, FFT passes of
   radix 10, 9 and 2) in a 6.72 nm box, which gives config 5's cell edge
-  (0.672 nm) and so its one-cell groups; both FFT launch shapes, the plane
-  path in chunks of lines as at 180^3;
+  (0.672 nm) and so its tile shape (one-cell neighbourhoods too dense for
+  two blocks per SM: one 32-warp block per SM, groups of 4 cells); both FFT
+  launch shapes, the plane path in chunks of lines as at 180^3;
 * config 4 in full: all 32 uneven lambda-window systems in one context.
 
 Each checks the neighbour pair set (array-equal to the oracle's, which is
@@ -95,10 +96,11 @@ def test_config5_shape(oracle, c5s, prec, fft_path):
     F0, E0, ref = _oracle(oracle, s)
     eng = _engine(s, precision=prec, fft_path=fft_path)
     lay = eng.layout()
-    # config 5's list and FFT geometry: one-cell groups, 0.672 nm cells,
-    # 180 = 10 x 9 x 2 per axis, and on the plane path x-planes larger than
-    # the shared-memory scratch
-    assert lay["cells_per_group"] == 1, lay
+    # config 5's list and FFT geometry: 0.672 nm cells whose one-cell
+    # neighbourhoods need one tile block per SM, groups of 4 cells (10 cells
+    # as 4 + 4 + 2), 180 = 10 x 9 x 2 per axis, and on the plane path
+    # x-planes larger than the shared-memory scratch
+    assert lay["cells_per_group"] == 4 and lay["hood_capacity"] > 4400, lay
     assert lay["cells_x"] == lay["cells_y"] == lay["cells_z"] == 10, lay
     assert lay["fft_radices"] == ((10, 9, 2),) * 3, lay
     assert lay["fft_path"] == fft_path, lay
