@@ -49,22 +49,28 @@ __global__ void k_assign(DevView v) {
     atomicAdd(&v.cell_count[key], 1);
 }
 
-// Exclusive scan of n ints by one block; out[n] = total.
-__global__ void k_scan(const Flags *flags, const int *in, int *out, int n) {
+// Exclusive scan of n ints by one block, four consecutive values per
+// thread per round; out[n] = total.
+__global__ void __launch_bounds__(1024) k_scan(const Flags *flags, const int *in, int *out, int n) {
     if (!flags->rebuild) return;
     __shared__ int wsum[32];
     __shared__ int carry;
     const unsigned full = 0xffffffffu;
-    int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
-    for (int base = 0; base < n; base += blockDim.x) {
-        int i = base + threadIdx.x;
-        int val = i < n ? in[i] : 0;
+    for (int base = 0; base < n; base += 4 * blockDim.x) {
+        const int i0 = base + 4 * threadIdx.x;
+        int a[4], val = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            a[k] = i0 + k < n ? in[i0 + k] : 0;
+            val += a[k];
+        }
         int xs = val;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            int y = __shfl_up_sync(full, xs, o);
+            const int y = __shfl_up_sync(full, xs, o);
             if (lane >= o) xs += y;
         }
         if (lane == 31) wsum[w] = xs;
@@ -73,16 +79,20 @@ __global__ void k_scan(const Flags *flags, const int *in, int *out, int n) {
             int ws = lane < nw ? wsum[lane] : 0;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
-                int y = __shfl_up_sync(full, ws, o);
+                const int y = __shfl_up_sync(full, ws, o);
                 if (lane >= o) ws += y;
             }
             wsum[lane] = ws;
         }
         __syncthreads();
         int prefix = carry + (w > 0 ? wsum[w - 1] : 0) + xs - val;
-        if (i < n) out[i] = prefix;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (i0 + k < n) out[i0 + k] = prefix;
+            prefix += a[k];
+        }
         __syncthreads();
-        if (threadIdx.x == blockDim.x - 1) carry = prefix + val;
+        if (threadIdx.x == blockDim.x - 1) carry = prefix;
         __syncthreads();
     }
     if (threadIdx.x == 0) out[n] = carry;
@@ -103,12 +113,15 @@ __global__ void k_scatter(DevView v) {
 // staged neighbourhood is sorted by z, which lets the list build bound its
 // scan to the atom's z window.  One warp per cell: each lane ranks its
 // elements against all of the cell's (shared memory); cells of more than
-// kSortMax atoms fall back to an insertion sort by one lane.
+// kSortMax atoms fall back to an insertion sort by one lane.  The key, a
+// fraction in [0, 1), is compared as the integer of its bits (the same
+// order for non-negative doubles), which keeps the n^2 comparisons off the
+// narrow FP64 pipe.
 constexpr int kSortWarps = 4, kSortMax = 64;
 
 __global__ void __launch_bounds__(kSortWarps * 32) k_cellsort(DevView v) {
     if (!v.flags->rebuild) return;
-    __shared__ double s_key[kSortWarps][kSortMax];
+    __shared__ long long s_key[kSortWarps][kSortMax];
     __shared__ int s_org[kSortWarps][kSortMax];
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int c = blockIdx.x * kSortWarps + warp;
@@ -119,17 +132,17 @@ __global__ void __launch_bounds__(kSortWarps * 32) k_cellsort(DevView v) {
         int s = v.slot_of[o];
         const SysDev &S = v.sys[v.sys_of[s]];
         double u = (v.z[s] - S.lb[2]) * S.invL[2];
-        return u - floor(u);
+        return __double_as_longlong(u - floor(u));
     };
     if (n > kSortMax) {
         if (lane == 0)
             for (int i = a + 1; i < a + n; ++i) {
                 int o = v.new_orig[i];
-                double k = key_of(o);
+                const long long k = key_of(o);
                 int j = i - 1;
                 while (j >= a) {
                     int oj = v.new_orig[j];
-                    double kj = key_of(oj);
+                    const long long kj = key_of(oj);
                     if (kj < k || (kj == k && oj < o)) break;
                     v.new_orig[j + 1] = oj;
                     --j;
@@ -146,10 +159,10 @@ __global__ void __launch_bounds__(kSortWarps * 32) k_cellsort(DevView v) {
     __syncwarp();
     int dst[2], val[2], m = 0;
     for (int e = lane; e < n; e += 32) {
-        double k = s_key[warp][e];
+        const long long k = s_key[warp][e];
         int o = s_org[warp][e], r = 0;
         for (int f = 0; f < n; ++f) {
-            double kf = s_key[warp][f];
+            const long long kf = s_key[warp][f];
             r += kf < k || (kf == k && s_org[warp][f] < o);
         }
         dst[m] = r;
@@ -196,8 +209,8 @@ __global__ void k_derive(DevView v, int gated) {
     cell_of(S, x, y, z, c);
     v.cell3[s] = c[0] | (c[1] << 10) | (c[2] << 20);
     double qs = v.q[s] * sqrt(kOne4PiEps0);
-    double sg = 0.5 * v.sig[s];
-    double ep = 2.0 * sqrt(v.eps[s]);
+    double sg = v.sig[s];  // sigma/2 and 2 sqrt(eps), formed at creation
+    double ep = v.eps[s];
     if (v.mixed) {
         double p[3] = {x, y, z};
         float o[3];

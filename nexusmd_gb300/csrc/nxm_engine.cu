@@ -50,7 +50,10 @@ __global__ void k_decide_graph(DevView v, cudaGraphConditionalHandle h) {
 
 // Context creation: positions given per atom as (x, y, z) into x, y, z;
 // 1/m (0 for a massless particle, VerletIntegration.cpp:37-45; the division
-// rounds as the host's); slot = original index until the first sort.
+// rounds as the host's); the LJ parameters as the combination rule uses
+// them, sigma/2 and 2 sqrt(eps) (NonbondedForce.cpp:504-513), once here
+// instead of at every list rebuild; slot = original index until the first
+// sort.
 __global__ void k_init_atoms(DevView v, const double *xyz) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N) return;
@@ -59,6 +62,8 @@ __global__ void k_init_atoms(DevView v, const double *xyz) {
     v.z[i] = xyz[3 * (size_t)i + 2];
     const double m = v.mass[i];
     v.invm[i] = m == 0.0 ? 0.0 : 1.0 / m;
+    v.sig[i] = 0.5 * v.sig[i];
+    v.eps[i] = 2.0 * sqrt(v.eps[i]);
     v.orig[i] = i;
     v.slot_of[i] = i;
 }

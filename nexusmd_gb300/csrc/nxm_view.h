@@ -29,7 +29,8 @@ struct DevView {
     int *slot_of;        // original index -> slot
     // state, slot order
     double *x, *y, *z, *vx, *vy, *vz, *mass, *invm;
-    double *q, *sig, *eps;          // raw per-atom parameters
+    double *q;                      // raw per-atom charge
+    double *sig, *eps;              // sigma/2 and 2 sqrt(eps), formed once at creation
     // derived per-slot inputs of the pair kernels
     float4 *pf;          // mixed: cell-relative offset (x,y,z), q * sqrt(ke)
     float2 *ljf;         // mixed: sigma/2, 2 sqrt(eps)
