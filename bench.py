@@ -357,6 +357,26 @@ def equilibrated_state(s, v0, kw, equil=4000, rescale_every=100):
     return x, v
 
 
+def skin_sweep(s, v0, kw, steps=1000, skins=(0.10, 0.12, 0.15)):
+    """Rebuild rate against list length: device ms per step over `steps`
+    steps from the same start for several list skins (the named config uses
+    0.1 nm, a rebuild at most every 10 steps)."""
+    from nexusmd_gb300.engine import Engine
+    out = {}
+    for skin in skins:
+        k = dict(kw, skin=skin)
+        eng = Engine(s, precision=1, **k)
+        eng.set_velocities(v0)
+        rb0 = eng.rebuilds()
+        ms = eng.time_steps(steps, DT_PS)
+        ph = eng.profile(20, DT_PS)
+        out["%.2f" % skin] = {"ms_per_step": sig(ms / steps), "rebuilds_per_1000": sig((eng.rebuilds() - rb0) * 1000 / steps),
+                              "list_radius_nm": sig(s.cutoff + skin), "pairs_phase_ms": sig(ph["pairs"], 3)}
+        eng.close()
+    out["steps"] = steps
+    return out
+
+
 def nve_drift(s, v0, kw, steps=10000, every=20, fp64_steps=0, equil=4000):
     """NVE total-energy drift without a thermostat from an equilibrated
     state: the mixed engine over `steps` steps and, when fp64_steps > 0, the
@@ -694,6 +714,7 @@ def native(args):
         del eng
         if not args.quick:
             out["nve_drift"] = nve_drift(s, v0, kw, fp64_steps=args.drift_fp64_steps)
+            out["skin_sweep"] = skin_sweep(s, v0, kw)
             ow = {"c1": other_workload(1, 2000, 50, local, check=not args.no_check),
                   "c2": other_workload(2, 1000, 50, local, check=not args.no_check, fp64_steps=50),
                   "c4": other_workload(4, 200, 10, local, check=not args.no_check),

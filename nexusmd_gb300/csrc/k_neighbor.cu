@@ -28,15 +28,6 @@ __device__ __forceinline__ void cell_of(const SysDev &S, double x, double y, dou
     }
 }
 
-__global__ void k_zero_cells(DevView v) {
-    if (!v.flags->rebuild) return;
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < v.total_cells) {
-        v.cell_count[c] = 0;
-        v.cell_fill[c] = 0;
-    }
-}
-
 __global__ void k_assign(DevView v) {
     if (!v.flags->rebuild) return;
     int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -127,6 +118,11 @@ __global__ void __launch_bounds__(kSortWarps * 32) k_cellsort(DevView v) {
     int c = blockIdx.x * kSortWarps + warp;
     if (c >= v.total_cells) return;
     int a = v.cell_start[c], n = v.cell_start[c + 1] - a;
+    // the cell's count and fill words, done with, start the next rebuild at zero
+    if (lane == 0) {
+        v.cell_count[c] = 0;
+        v.cell_fill[c] = 0;
+    }
     if (n <= 1) return;
     auto key_of = [&](int o) {
         int s = v.slot_of[o];
@@ -184,33 +180,17 @@ __global__ void k_permute_gather(DevView v) {
     for (int k = 0; k < kPermArrays; ++k) v.tmp[(size_t)k * v.N + s] = src[k][so];
 }
 
-__global__ void k_permute_scatter(DevView v) {
-    if (!v.flags->rebuild) return;
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= v.N) return;
-    double *dst[kPermArrays] = {v.x, v.y, v.z, v.vx, v.vy, v.vz, v.mass, v.invm, v.q, v.sig, v.eps};
-#pragma unroll
-    for (int k = 0; k < kPermArrays; ++k) dst[k][s] = v.tmp[(size_t)k * v.N + s];
-    int o = v.new_orig[s];
-    v.orig[s] = o;
-    v.slot_of[o] = s;
-}
-
 // Per-slot derived inputs: cell coordinates, cell-relative FP32 offsets,
 // scaled charges and combined LJ parameters (NonbondedForce.cpp:504-513:
-// sigma/2 and 2 sqrt(eps)), and the rebuild-time reference positions.
-__global__ void k_derive(DevView v, int gated) {
-    if (gated && !v.flags->rebuild) return;
-    int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= v.N) return;
+// sigma/2 and 2 sqrt(eps), kept in sig / eps since creation), and the
+// rebuild-time reference positions.
+__device__ __forceinline__ void derive_slot(const DevView &v, int s, double x, double y, double z, double q,
+                                            double sg, double ep) {
     const SysDev &S = v.sys[v.sys_of[s]];
-    double x = v.x[s], y = v.y[s], z = v.z[s];
     int c[3];
     cell_of(S, x, y, z, c);
     v.cell3[s] = c[0] | (c[1] << 10) | (c[2] << 20);
-    double qs = v.q[s] * sqrt(kOne4PiEps0);
-    double sg = v.sig[s];  // sigma/2 and 2 sqrt(eps), formed at creation
-    double ep = v.eps[s];
+    double qs = q * sqrt(kOne4PiEps0);
     if (v.mixed) {
         double p[3] = {x, y, z};
         float o[3];
@@ -222,11 +202,6 @@ __global__ void k_derive(DevView v, int gated) {
         v.pf[s] = make_float4(o[0], o[1], o[2], (float)qs);
         v.oref[s] = make_float4(o[0], o[1], o[2], (float)qs);
         v.ljf[s] = make_float2((float)sg, (float)ep);
-    } else {
-        v.qs[s] = qs;
-        v.ljd[s] = make_double2(sg, ep);
-    }
-    if (v.mixed) {
         // the mixed integrator's skin test and cell offsets take
         // displacements from these in fixed point (fix40)
         long long *x40 = reinterpret_cast<long long *>(v.xref);
@@ -234,10 +209,38 @@ __global__ void k_derive(DevView v, int gated) {
         x40[v.N + s] = fix40(y);
         x40[2 * v.N + s] = fix40(z);
     } else {
+        v.qs[s] = qs;
+        v.ljd[s] = make_double2(sg, ep);
         v.xref[s] = x;
         v.xref[v.N + s] = y;
         v.xref[2 * v.N + s] = z;
     }
+}
+
+// The permuted arrays into place, the slot maps, and the slot's derived
+// inputs from the same values.
+__global__ void k_permute_scatter(DevView v) {
+    if (!v.flags->rebuild) return;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= v.N) return;
+    double *dst[kPermArrays] = {v.x, v.y, v.z, v.vx, v.vy, v.vz, v.mass, v.invm, v.q, v.sig, v.eps};
+    double val[kPermArrays];
+#pragma unroll
+    for (int k = 0; k < kPermArrays; ++k) {
+        val[k] = v.tmp[(size_t)k * v.N + s];
+        dst[k][s] = val[k];
+    }
+    int o = v.new_orig[s];
+    v.orig[s] = o;
+    v.slot_of[o] = s;
+    derive_slot(v, s, val[0], val[1], val[2], val[8], val[9], val[10]);
+}
+
+// The derived inputs alone (context creation, new positions).
+__global__ void k_derive(DevView v) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= v.N) return;
+    derive_slot(v, s, v.x[s], v.y[s], v.z[s], v.q[s], v.sig[s], v.eps[s]);
 }
 
 __global__ void k_remap(DevView v) {
@@ -276,7 +279,7 @@ __global__ void k_remap(DevView v) {
 static inline int blocks(long long n, int t) { return (int)((n + t - 1) / t); }
 
 void launch_derive_inputs(const DevView &v, cudaStream_t st) {
-    k_derive<<<blocks(v.N, 256), 256, 0, st>>>(v, 0);
+    k_derive<<<blocks(v.N, 256), 256, 0, st>>>(v);
 }
 
 void launch_remap_terms(const DevView &v, cudaStream_t st) {
@@ -285,14 +288,12 @@ void launch_remap_terms(const DevView &v, cudaStream_t st) {
 }
 
 void launch_nlist_rebuild(const DevView &v, cudaStream_t st) {
-    k_zero_cells<<<blocks(v.total_cells, 256), 256, 0, st>>>(v);
     k_assign<<<blocks(v.N, 256), 256, 0, st>>>(v);
     k_scan<<<1, 1024, 0, st>>>(v.flags, v.cell_count, v.cell_start, v.total_cells);
     k_scatter<<<blocks(v.N, 256), 256, 0, st>>>(v);
     k_cellsort<<<blocks(v.total_cells, kSortWarps), kSortWarps * 32, 0, st>>>(v);
     k_permute_gather<<<blocks(v.N, 256), 256, 0, st>>>(v);
     k_permute_scatter<<<blocks(v.N, 256), 256, 0, st>>>(v);
-    k_derive<<<blocks(v.N, 256), 256, 0, st>>>(v, 1);
     long long nt = (long long)v.nb + v.na + v.nt + v.nex + v.nxc;
     if (nt > 0) k_remap<<<blocks(nt, 256), 256, 0, st>>>(v);
     launch_build(v, st);

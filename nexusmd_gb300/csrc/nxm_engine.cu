@@ -355,7 +355,7 @@ T *Engine::dalloc(size_t n) {
             alloc_failed_ = true;
             return nullptr;
         }
-        cudaMemset(p, 0, b);
+        cudaMemsetAsync(p, 0, b, st_);  // in the order of the set-up's work on the stream
         allocs_.push_back(p);
         create_ms_[6] += now_ms() - t0;
         return static_cast<char *>(p);
@@ -1358,7 +1358,7 @@ std::string Engine::build_graph_timed(double dt, int report) {
 // One step of report kind `report` (0 none, 1 energies and the x/v/F
 // snapshot, 2 / 3 a frame into frame buffer A / B).
 std::string Engine::one_step(double dt, int report) {
-    launches_per_rebuild_ = 10;  // kernels of one list rebuild
+    launches_per_rebuild_ = 8;  // kernels of one list rebuild
     if (!force_rebuild_) {
         StepGraph &G = graph_[report];
         if (!G.ok || G.dt != dt) {
