@@ -165,7 +165,9 @@ static void bspline_moduli(int K, std::vector<double> &mod) {
 // of the system to the batch CSR (eoff, elst), indices shifted by `off`, and
 // the pairs with j > i to ex_pairs.  Flat arrays only: the bonds' adjacency
 // by a counting sort, one breadth-first search per atom into a shared
-// buffer, then a merge with the atom's sorted exception partners.
+// buffer, then a merge with the atom's sorted exception partners.  The
+// creation builds the same sets on the device (k_exclusions_build.cu); this
+// host form serves a batch with a row longer than the device search holds.
 static std::string exclusion_rows(const HostSystem &s, int off, std::vector<int> &eoff, std::vector<int> &elst,
                                   std::vector<int2> &ex_pairs) {
     const int n = s.n;
