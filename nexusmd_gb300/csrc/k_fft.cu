@@ -21,6 +21,7 @@
 // a shared-memory copy of the axis's table; lines in shared memory have an odd
 // stride (in complex words) so that column accesses do not conflict on banks.
 #include <algorithm>
+#include <cstring>
 #include <mutex>
 
 #include "nxm_fft.h"
@@ -675,7 +676,7 @@ static void raise_all(const FftPlan &p, int base) {
     }
 }
 
-void fft_plan_build(FftPlan &p, int mixed) {
+void fft_plan_build(FftPlan &p, int mixed, cudaStream_t st) {
     // sizes and factorizations (lengths must be 2^a 3^b 5^c, checked by the caller)
     std::vector<FftWork> z, y, x, pl;
     p.kmax = 0;
@@ -714,29 +715,40 @@ void fft_plan_build(FftPlan &p, int mixed) {
     p.plane_chunked = p.plane_ok && p.scr < scr;
     if (!p.plane_ok) p.plane = 0;
     p.smem_plane = ((size_t)p.twcap + p.qcap + 2 * (size_t)std::max(p.scr, 0)) * csz;
-    // device buffers are kept across rebuilds of the same plan (the autotuner
-    // rebuilds it per candidate) and grown when too small
-    auto ensure = [](auto *&ptr, size_t &cap, size_t n) {
-        if (n <= cap && ptr) return;
-        cudaFree(ptr);
-        ptr = nullptr;
-        cudaMalloc(&ptr, sizeof(*ptr) * n);
-        cap = n;
-    };
-    ensure(p.dsys, p.cap[0], (size_t)std::max(p.S, 1));
-    cudaMemcpy(p.dsys, p.hsys.data(), sizeof(FftSysDev) * p.S, cudaMemcpyHostToDevice);
+    // The per-system geometry and the work lists share one device buffer,
+    // kept across rebuilds of the plan (the autotuner rebuilds it per
+    // candidate) and grown when too small; they are copied in the order of
+    // the stream that runs the transforms.
     p.nz = (int)z.size();
     p.ny = (int)y.size();
     p.nx = (int)x.size();
     p.npl = (int)pl.size();
-    ensure(p.zwork, p.cap[1], (size_t)p.nz + 1);
-    ensure(p.ywork, p.cap[2], (size_t)p.ny + 1);
-    ensure(p.xwork, p.cap[3], (size_t)p.nx + 1);
-    ensure(p.pwork, p.cap[4], (size_t)p.npl + 1);
-    cudaMemcpy(p.zwork, z.data(), sizeof(FftWork) * p.nz, cudaMemcpyHostToDevice);
-    cudaMemcpy(p.ywork, y.data(), sizeof(FftWork) * p.ny, cudaMemcpyHostToDevice);
-    cudaMemcpy(p.xwork, x.data(), sizeof(FftWork) * p.nx, cudaMemcpyHostToDevice);
-    cudaMemcpy(p.pwork, pl.data(), sizeof(FftWork) * p.npl, cudaMemcpyHostToDevice);
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t bs = al(sizeof(FftSysDev) * std::max(p.S, 1)), bz = al(sizeof(FftWork) * (p.nz + 1)),
+                 by = al(sizeof(FftWork) * (p.ny + 1)), bx = al(sizeof(FftWork) * (p.nx + 1)),
+                 bp = al(sizeof(FftWork) * (p.npl + 1)), need = bs + bz + by + bx + bp;
+    if (need > p.cap || !p.buf) {
+        cudaFree(p.buf);
+        p.buf = nullptr;
+        p.cap = 0;
+        if (cudaMalloc(&p.buf, need) == cudaSuccess) p.cap = need;
+    }
+    char *b = static_cast<char *>(p.buf);
+    p.dsys = reinterpret_cast<FftSysDev *>(b);
+    p.zwork = reinterpret_cast<FftWork *>(b + bs);
+    p.ywork = reinterpret_cast<FftWork *>(b + bs + bz);
+    p.xwork = reinterpret_cast<FftWork *>(b + bs + bz + by);
+    p.pwork = reinterpret_cast<FftWork *>(b + bs + bz + by + bx);
+    if (p.buf) {
+        // one copy from a host image of the buffer
+        std::vector<char> img(need, 0);
+        std::memcpy(img.data(), p.hsys.data(), sizeof(FftSysDev) * p.S);
+        std::memcpy(img.data() + bs, z.data(), sizeof(FftWork) * p.nz);
+        std::memcpy(img.data() + bs + bz, y.data(), sizeof(FftWork) * p.ny);
+        std::memcpy(img.data() + bs + bz + by, x.data(), sizeof(FftWork) * p.nx);
+        std::memcpy(img.data() + bs + bz + by + bx, pl.data(), sizeof(FftWork) * p.npl);
+        cudaMemcpyAsync(p.buf, img.data(), need, cudaMemcpyHostToDevice, st);
+    }
     if (mixed)
         raise_all<float2, int, float>(p, 0);
     else
@@ -744,12 +756,9 @@ void fft_plan_build(FftPlan &p, int mixed) {
 }
 
 void fft_plan_free(FftPlan &p) {
-    cudaFree(p.dsys);
-    cudaFree(p.zwork);
-    cudaFree(p.ywork);
-    cudaFree(p.xwork);
-    cudaFree(p.pwork);
-    for (size_t &c : p.cap) c = 0;
+    cudaFree(p.buf);
+    p.buf = nullptr;
+    p.cap = 0;
     p.dsys = nullptr;
     p.zwork = p.ywork = p.xwork = p.pwork = nullptr;
 }

@@ -337,34 +337,46 @@ static void launch_influence(void *eterm, int mixed, long long coff, const doubl
 
 // ------------------------------------------------------------ engine
 
+static size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
+
 static double now_ms() {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-// Zeroed device arrays.  Arrays up to a quarter of a chunk come out of 32 MB
-// chunks, 256-byte aligned (one cudaMalloc and one memset per chunk);
-// larger ones get an allocation of their own.  Freed with the engine.
+// Zeroed device arrays, 256-byte aligned, carved out of chunks: one
+// cudaMalloc (~30 us whatever its size) and one memset per chunk, not per
+// array.  The set-up first reserves one chunk sized for all of the context's
+// arrays; what does not fit comes out of further 32 MB chunks, or gets a
+// chunk of its own above 8 MB.  Freed with the engine.
 constexpr size_t kArenaChunk = 32u << 20;
+
+char *Engine::chunk(size_t b) {
+    const double t0 = now_ms();
+    void *p = nullptr;
+    if (cudaMalloc(&p, b) != cudaSuccess) {
+        alloc_failed_ = true;
+        return nullptr;
+    }
+    cudaMemsetAsync(p, 0, b, st_);  // in the order of the set-up's work on the stream
+    allocs_.push_back(p);
+    create_ms_[6] += now_ms() - t0;
+    return static_cast<char *>(p);
+}
+
+void Engine::arena_reserve(size_t b) {
+    b = (b + 255) & ~(size_t)255;
+    if (b <= arena_left_) return;
+    arena_ptr_ = chunk(b);
+    arena_left_ = arena_ptr_ ? b : 0;
+}
 
 template <typename T>
 T *Engine::dalloc(size_t n) {
     if (n == 0) n = 1;
     const size_t bytes = (n * sizeof(T) + 255) & ~(size_t)255;
-    auto fresh = [&](size_t b) -> char * {
-        const double t0 = now_ms();
-        void *p = nullptr;
-        if (cudaMalloc(&p, b) != cudaSuccess) {
-            alloc_failed_ = true;
-            return nullptr;
-        }
-        cudaMemsetAsync(p, 0, b, st_);  // in the order of the set-up's work on the stream
-        allocs_.push_back(p);
-        create_ms_[6] += now_ms() - t0;
-        return static_cast<char *>(p);
-    };
-    if (bytes > kArenaChunk / 4) return reinterpret_cast<T *>(fresh(bytes));
     if (arena_left_ < bytes) {
-        arena_ptr_ = fresh(kArenaChunk);
+        if (bytes > kArenaChunk / 4) return reinterpret_cast<T *>(chunk(bytes));
+        arena_ptr_ = chunk(kArenaChunk);
         arena_left_ = arena_ptr_ ? kArenaChunk : 0;
         if (!arena_ptr_) return nullptr;
     }
@@ -377,17 +389,15 @@ T *Engine::dalloc(size_t n) {
 Engine::~Engine() {
     if (st_) cudaStreamSynchronize(st_);
     free_frames();
-    for (int b = 0; b < 2; ++b) {
-        if (frame_x_[b]) cudaFree(frame_x_[b]);
-        if (frame_E_[b]) cudaFree(frame_E_[b]);
+    for (int b = 0; b < 2; ++b)
         if (buf_free_[b]) cudaEventDestroy(buf_free_[b]);
-    }
     if (step_done_) cudaEventDestroy(step_done_);
+    if (ev_setup_) cudaEventDestroy(ev_setup_);
     if (st_copy_) cudaStreamDestroy(st_copy_);
     free_graphs();
     for (void *p : allocs_) cudaFree(p);
     fft_plan_free(plan_);
-    if (h_E_) cudaFreeHost(h_E_);  // h_flags_ lies in the same block
+    if (h_E_) cudaFreeHost(h_E_);  // h_flags_, h_tail_ and the built-in frame ring lie in the same block
     if (ev_fork_) cudaEventDestroy(ev_fork_);
     if (ev_join_) cudaEventDestroy(ev_join_);
     if (st_pme_) cudaStreamDestroy(st_pme_);
@@ -621,11 +631,53 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     cudaStreamCreateWithFlags(&st_pme_, cudaStreamNonBlocking);
     cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming);
+    energies_.assign((size_t)S * E_SLOTS, 0.0);
+    {
+        // pinned host memory in one block (pinning costs ~0.1 ms a call):
+        // the energy words, the flags, the exclusion build's totals and the
+        // default two-slot frame ring of nxm_step_async
+        const size_t be = al256(sizeof(long long) * energies_.size()), bf = al256(sizeof(Flags)), bt = 256;
+        void *hp = nullptr;
+        if (cudaMallocHost(&hp, be + bf + bt + 2 * frame_slot_bytes()) != cudaSuccess)
+            return "device: pinned host allocation failed";
+        h_E_ = static_cast<long long *>(hp);
+        h_flags_ = reinterpret_cast<int *>(static_cast<char *>(hp) + be);
+        h_tail_ = reinterpret_cast<int *>(static_cast<char *>(hp) + be + bf);
+        ring_builtin_ = static_cast<char *>(hp) + be + bf + bt;
+    }
+    // the frame copies' stream and events
+    for (int b = 0; b < 2; ++b) cudaEventCreateWithFlags(&buf_free_[b], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&step_done_, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&ev_setup_, cudaEventDisableTiming);
+    cudaStreamCreateWithFlags(&st_copy_, cudaStreamNonBlocking);
     v_ = DevView{};
     v_.N = N_;
     v_.S = S;
     v_.mixed = mixed_;
     v_.stride = stride;
+    {
+        // one reservation for the context's device arrays (an upper
+        // estimate; a shortfall comes out of further chunks): per atom the
+        // state, derived inputs, cell keys, exclusion build, PME stencils,
+        // snapshots and frames (~600 B) and the list; per cell, group, term,
+        // exception and grid point their tables
+        size_t nb = 0, na = 0, nt = 0, nx = 0, ngr = 0;
+        for (int s = 0; s < S; ++s) {
+            const HostSystem &h = systems[s];
+            nb += h.bonds.size() / 2;
+            na += h.angles.size() / 3;
+            nt += h.torsions.size() / 4;
+            nx += h.exc.size() / 2;
+            const SysDev &D = sysd_[s];
+            ngr += (size_t)D.nc[0] * D.nc[1] * ((D.nc[2] + group_g[s] - 1) / group_g[s]);
+        }
+        const size_t est = (size_t)N_ * (600 + 2 * (size_t)stride) + 12 * ((size_t)cell_off + 1) +
+                           ngr * (sizeof(CellGroup) + 4 * (size_t)kGroupSpanWords + 8) +
+                           (size_t)S * (kDtabStride * sizeof(float4) + 24 * E_SLOTS + sizeof(SysDev)) +
+                           8 * (size_t)cg_total + 56 * nb + 56 * na + 60 * nt + 88 * nx + 16 * (size_t)roff +
+                           24 * (size_t)coff + 24 * (size_t)tw_total + (256u << 10);
+        arena_reserve(est);
+    }
     SysDev *dsys = dalloc<SysDev>(S);
     cudaMemcpyAsync(dsys, sysd_.data(), sizeof(SysDev) * S, cudaMemcpyHostToDevice, st_);
     v_.sys = dsys;
@@ -765,6 +817,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     // j > i of the systems with the nonbonded force, built on the device
     // (k_exclusions_build.cu); a row too long for it: built on the host
     bool ex_on_host = false;
+    ExclBuild B{};
     {
         const double t0 = now_ms();
         std::vector<int2> eb;  // every bond, batch-global (the search ignores the force mask)
@@ -790,7 +843,6 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         v_.nxc = (int)xc_pairs.size();
         v_.xc_orig = dalloc<int2>(v_.nxc);
         if (v_.nxc) up(v_.xc_orig, xc_pairs.data(), sizeof(int2) * v_.nxc);
-        ExclBuild B{};
         B.n = N_;
         B.nb = (int)eb.size();
         B.nx = v_.nxc;
@@ -822,33 +874,14 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         if (alloc_failed_) return "device allocation failed (exclusions)";
         cudaMemsetAsync(B.overflow, 0, sizeof(int), st_);
         launch_exclusions_count(B, st_);
-        int tail[3] = {0, 0, 0};
-        cudaMemcpyAsync(tail, B.eoff + N_, sizeof(int), cudaMemcpyDeviceToHost, st_);
-        cudaMemcpyAsync(tail + 1, B.poff + N_, sizeof(int), cudaMemcpyDeviceToHost, st_);
-        cudaMemcpyAsync(tail + 2, B.overflow, sizeof(int), cudaMemcpyDeviceToHost, st_);
-        cudaStreamSynchronize(st_);
+        // the totals (list length, pair count, overflow) are read once the
+        // host has prepared the terms and the PME tables (below)
+        cudaMemcpyAsync(h_tail_, B.eoff + N_, sizeof(int), cudaMemcpyDeviceToHost, st_);
+        cudaMemcpyAsync(h_tail_ + 1, B.poff + N_, sizeof(int), cudaMemcpyDeviceToHost, st_);
+        cudaMemcpyAsync(h_tail_ + 2, B.overflow, sizeof(int), cudaMemcpyDeviceToHost, st_);
+        cudaEventRecord(ev_setup_, st_);
         std::string e = check("exclusions");
         if (!e.empty()) return e;
-        if (tail[2]) {
-            ex_on_host = true;
-            int o = 0;
-            for (const HostSystem &h : systems) {
-                e = exclusion_rows(h, o, eoff, elst, ex_pairs);
-                if (!e.empty()) return e;
-                o += h.n;
-            }
-            v_.excl_off = dalloc<int>(N_ + 1);
-            v_.excl_lst = dalloc<int>(std::max<size_t>(elst.size(), 1));
-            up(v_.excl_off, eoff.data(), sizeof(int) * (N_ + 1));
-            if (!elst.empty()) up(v_.excl_lst, elst.data(), sizeof(int) * elst.size());
-        } else {
-            v_.excl_off = B.eoff;
-            v_.excl_lst = dalloc<int>(std::max(tail[0], 1));
-            v_.nex = tail[1];
-            v_.ex_orig = dalloc<int2>(std::max(v_.nex, 1));
-            if (alloc_failed_) return "device allocation failed (exclusions)";
-            launch_exclusions_fill(B, v_.excl_lst, v_.ex_orig, st_);
-        }
         create_ms_[8] = now_ms() - t0;
     }
 
@@ -947,18 +980,6 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         for (int k = 0; k < 3; ++k)
             if (cnt[k]) k_params_f32<<<(cnt[k] + 255) / 256, 256, 0, st_>>>(pr[k].first, pr[k].second, cnt[k]);
     }
-    // exclusion correction pairs (host-built sets): only for systems with
-    // nonbonded enabled
-    if (ex_on_host) {
-        std::vector<int2> keep;
-        for (auto &e : ex_pairs)
-            if (sysh_[sys_of[e.x]].force_mask & NXM_FORCE_NONBONDED) keep.push_back(e);
-        ex_pairs.swap(keep);
-        v_.nex = (int)ex_pairs.size();
-        v_.ex_orig = dalloc<int2>(v_.nex);
-        if (v_.nex) up(v_.ex_orig, ex_pairs.data(), sizeof(int2) * v_.nex);
-    }
-    v_.ex_slot = dalloc<int2>(v_.nex);
     v_.xc_slot = dalloc<int2>(v_.nxc);
     v_.xc_prm = dalloc<double4>(v_.nxc);
     if (v_.nxc) up(v_.xc_prm, xc_prm.data(), sizeof(double4) * v_.nxc);
@@ -977,6 +998,8 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     for (auto &h : sysh_) any_nb |= (h.force_mask & NXM_FORCE_NONBONDED) != 0;
     v_.total_grid = roff;
     v_.total_cgrid = coff;
+    bool tuned = false;
+    int tv[5] = {0, 0, 0, 0, 0};
     if (any_nb) {
         v_.grid_acc = mixed_ ? (void *)dalloc<int>(roff) : (void *)dalloc<double>(roff);
         v_.grid_real = mixed_ ? (void *)dalloc<float>(roff) : (void *)dalloc<double>(roff);
@@ -1033,13 +1056,62 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         v_.pme_frac = mixed_ ? (void *)dalloc<float4>(N_) : (void *)dalloc<double2>(2 * (size_t)N_);
         // FFT work lists only for systems with nonbonded forces: systems
         // without them keep an empty grid that no block touches
-        fft_plan_build(plan_, mixed_);
-        plan_.plane = plan_.plane_ok && fft_path_ == 2;
+        // launch shapes an earlier context of the same shapes tuned, else
+        // the defaults until the autotuner has timed the candidates
+        tuned = opt.autotune && tune_lookup(tv);
+        if (tuned) {
+            plan_.zlines = tv[0];
+            plan_.cols = tv[1];
+        }
+        fft_plan_build(plan_, mixed_, st_);
+        plan_.plane = tuned ? (tv[2] && plan_.plane_ok) : (plan_.plane_ok && fft_path_ == 2);
+        if (tuned) plan_.plane_threads = tv[3];
         tune_[0] = plan_.plane ? 0 : plan_.zlines;
+        tune_[1] = plan_.cols;
+        if (tuned) tune_[2] = tv[4];
     }
-    v_.pme_block = 128;
+    v_.pme_block = tuned ? tv[4] : 128;
     const double t_pme = now_ms();
     create_ms_[2] = t_pme - t_dev;
+    {
+        // the exclusion sets: their build on the device ran while the host
+        // prepared the terms and the PME tables; a row too long for it, or a
+        // batch beyond its scans' reach, is built on the host instead
+        const double t0 = now_ms();
+        cudaEventSynchronize(ev_setup_);
+        std::string e = check("exclusions");
+        if (!e.empty()) return e;
+        if (h_tail_[2]) {
+            ex_on_host = true;
+            int o = 0;
+            for (const HostSystem &h : systems) {
+                e = exclusion_rows(h, o, eoff, elst, ex_pairs);
+                if (!e.empty()) return e;
+                o += h.n;
+            }
+            v_.excl_off = dalloc<int>(N_ + 1);
+            v_.excl_lst = dalloc<int>(std::max<size_t>(elst.size(), 1));
+            up(v_.excl_off, eoff.data(), sizeof(int) * (N_ + 1));
+            if (!elst.empty()) up(v_.excl_lst, elst.data(), sizeof(int) * elst.size());
+            // exclusion correction pairs: only for systems with nonbonded enabled
+            std::vector<int2> keep;
+            for (auto &x : ex_pairs)
+                if (sysh_[sys_of[x.x]].force_mask & NXM_FORCE_NONBONDED) keep.push_back(x);
+            ex_pairs.swap(keep);
+            v_.nex = (int)ex_pairs.size();
+            v_.ex_orig = dalloc<int2>(v_.nex);
+            if (v_.nex) up(v_.ex_orig, ex_pairs.data(), sizeof(int2) * v_.nex);
+        } else {
+            v_.excl_off = B.eoff;
+            v_.excl_lst = dalloc<int>(std::max(h_tail_[0], 1));
+            v_.nex = h_tail_[1];
+            v_.ex_orig = dalloc<int2>(std::max(v_.nex, 1));
+            if (alloc_failed_) return "device allocation failed (exclusions)";
+            launch_exclusions_fill(B, v_.excl_lst, v_.ex_orig, st_);
+        }
+        v_.ex_slot = dalloc<int2>(v_.nex);
+        create_ms_[8] += now_ms() - t0;
+    }
     // systems without nonbonded forces: zero their charges in the PME and
     // pair paths by skipping them entirely (no list, no grid)
     v_.E = dalloc<long long>((size_t)S * E_SLOTS);
@@ -1052,32 +1124,34 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     v_.snap_x = dalloc<double>(3 * (size_t)N_);
     v_.snap_v = dalloc<double>(3 * (size_t)N_);
     v_.snap_f = dalloc<double>(3 * (size_t)N_);
+    // frame steps' device buffers A and B (nxm_step_async)
+    for (int b = 0; b < 2; ++b) {
+        frame_x_[b] = dalloc<double>(3 * (size_t)N_);
+        frame_E_[b] = dalloc<long long>(energies_.size());
+    }
     v_.skin_half2 = skin > 0 ? 0.25 * skin * skin : 0.0;
     v_.force_mask = 0;
     for (auto &h : sysh_) v_.force_mask |= h.force_mask;
     v_.any_switch = 0;
     for (auto &d : sysd_) v_.any_switch |= d.use_switch ? 1 : 0;
-    // the energy words and the flags in one pinned block (pinning is slow per call)
-    {
-        void *hp = nullptr;
-        const size_t be = (sizeof(long long) * S * E_SLOTS + 255) & ~(size_t)255;
-        if (cudaMallocHost(&hp, be + sizeof(Flags)) != cudaSuccess) return "device: pinned host allocation failed";
-        h_E_ = static_cast<long long *>(hp);
-        h_flags_ = reinterpret_cast<int *>(static_cast<char *>(hp) + be);
-    }
-    energies_.assign((size_t)S * E_SLOTS, 0.0);
     if (alloc_failed_) return "device allocation failed";
     launch_derive_inputs(v_, st_);
     force_rebuild_ = true;
     std::string e = check("set-up");
     if (!e.empty()) return e;
-    cudaStreamSynchronize(st_);
-    e = check("set-up");
-    if (!e.empty()) return e;
     // the allocations and uploads after the PME tables count with [1]
     const double t_rest = now_ms();
     create_ms_[1] += t_rest - t_pme;
-    if (opt.autotune && (v_.force_mask & NXM_FORCE_NONBONDED) && plan_.nz) e = autotune();
+    // Without candidates to time, creation returns with its last kernels
+    // still queued: the next call that waits for the device reports a
+    // failure of theirs.
+    autotune_cached_ = tuned ? 1 : 0;
+    if (opt.autotune && !tuned && (v_.force_mask & NXM_FORCE_NONBONDED) && plan_.nz) {
+        cudaStreamSynchronize(st_);
+        e = check("set-up");
+        if (!e.empty()) return e;
+        e = autotune();
+    }
     create_ms_[3] = now_ms() - t_rest;
     create_ms_[5] = create_ms_[0] + create_ms_[1] + create_ms_[2] + create_ms_[3];
     return e;
@@ -1112,28 +1186,23 @@ std::map<TuneKey, TuneVal> g_tune_cache;
 // The neighbour-list cell groups are not tuned: their size changes the
 // summation order of the pair forces, and a choice that followed timing
 // noise would break run-to-run bit reproducibility.
+bool Engine::tune_lookup(int out[5]) {
+    TuneKey key{device_, mixed_, fft_path_, N_, {}};
+    for (auto &h : sysh_)
+        for (int d = 0; d < 3; ++d) key.grids.push_back(h.K[d]);
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it == g_tune_cache.end()) return false;
+    const TuneVal &t = it->second;
+    const int v[5] = {t.zlines, t.cols, t.plane, t.plane_threads, t.pme_block};
+    std::copy(v, v + 5, out);
+    return true;
+}
+
 std::string Engine::autotune() {
     TuneKey key{device_, mixed_, fft_path_, N_, {}};
     for (auto &h : sysh_)
         for (int d = 0; d < 3; ++d) key.grids.push_back(h.K[d]);
-    {
-        std::lock_guard<std::mutex> lock(g_tune_mu);
-        auto it = g_tune_cache.find(key);
-        if (it != g_tune_cache.end()) {
-            const TuneVal &t = it->second;
-            plan_.zlines = t.zlines;
-            plan_.cols = t.cols;
-            fft_plan_build(plan_, mixed_);
-            plan_.plane = t.plane;
-            plan_.plane_threads = t.plane_threads;
-            v_.pme_block = t.pme_block;
-            tune_[0] = plan_.plane ? 0 : t.zlines;
-            tune_[1] = t.cols;
-            tune_[2] = t.pme_block;
-            autotune_cached_ = 1;
-            return check("autotune (cached)");
-        }
-    }
     cudaEvent_t a, b;
     cudaEventCreate(&a);
     cudaEventCreate(&b);
@@ -1162,7 +1231,7 @@ std::string Engine::autotune() {
             if (!try_line && zl != 16) continue;  // the z blocking is unused on the plane path
             plan_.zlines = zl;
             plan_.cols = cols;
-            fft_plan_build(plan_, mixed_);
+            fft_plan_build(plan_, mixed_, st_);
             for (int plane = 0; plane < 2; ++plane) {
                 if (plane ? !(try_plane && zl == 16) : !try_line) continue;
                 plan_.plane = plane;
@@ -1183,7 +1252,7 @@ std::string Engine::autotune() {
     }
     plan_.zlines = bz;
     plan_.cols = bc;
-    fft_plan_build(plan_, mixed_);
+    fft_plan_build(plan_, mixed_, st_);
     plan_.plane = bp;
     plan_.plane_threads = bpt;
     best = 1e30f;
@@ -1225,14 +1294,14 @@ std::string Engine::set_positions(const double *xyz) {
     if (N_ > 0) k_state_to_slots<<<(N_ + 255) / 256, 256, 0, st_>>>(v_, v_.tmp, v_.x, v_.y, v_.z);
     launch_derive_inputs(v_, st_);
     force_rebuild_ = true;
-    cudaStreamSynchronize(st_);
     return check("set_positions");
 }
 
+// The caller's array is consumed when the upload returns (pageable memory is
+// staged); the gather runs in the stream's order before the next step.
 std::string Engine::set_velocities(const double *xyz) {
     cudaMemcpyAsync(v_.tmp, xyz, sizeof(double) * 3 * (size_t)N_, cudaMemcpyHostToDevice, st_);
     if (N_ > 0) k_state_to_slots<<<(N_ + 255) / 256, 256, 0, st_>>>(v_, v_.tmp, v_.vx, v_.vy, v_.vz);
-    cudaStreamSynchronize(st_);
     return check("set_velocities");
 }
 
@@ -1435,35 +1504,31 @@ DevView Engine::view_for(int kind) const {
     return v;
 }
 
+size_t Engine::frame_slot_bytes() const {
+    return al256(sizeof(double) * 3 * (size_t)N_) + al256(sizeof(long long) * energies_.size()) + al256(sizeof(Flags));
+}
+
 std::string Engine::frames_init(int depth) {
     if (depth < 1 || depth > 64) return "frame ring depth must be 1..64";
     if (ring_pending_) return "frames still pending: wait for them first";
     free_frames();
-    // one pinned allocation for all slots (pinning is slow per call):
-    // per slot the positions, the energy words and the flags, 256-byte aligned
-    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    const size_t bx = al(sizeof(double) * 3 * (size_t)N_), be = al(sizeof(long long) * energies_.size()),
-                 bf = al(sizeof(Flags)), slot = bx + be + bf;
-    if (cudaMallocHost(&ring_mem_, slot * depth) != cudaSuccess) {
-        ring_mem_ = nullptr;
-        return "device: pinned frame buffers could not be allocated";
-    }
-    if (!st_copy_) {
-        // device frame buffers, the copy stream and its events: once per context
-        for (int b = 0; b < 2; ++b) {
-            if (cudaMalloc(&frame_x_[b], sizeof(double) * 3 * (size_t)N_) != cudaSuccess ||
-                cudaMalloc(&frame_E_[b], sizeof(long long) * energies_.size()) != cudaSuccess ||
-                cudaEventCreateWithFlags(&buf_free_[b], cudaEventDisableTiming) != cudaSuccess)
-                return "device: frame buffers could not be allocated";
-            buf_used_[b] = false;
+    // per slot the positions, the energy words and the flags, 256-byte
+    // aligned; two slots come with the context's pinned block, a deeper ring
+    // gets one pinned allocation of its own
+    const size_t bx = al256(sizeof(double) * 3 * (size_t)N_), be = al256(sizeof(long long) * energies_.size()),
+                 slot = frame_slot_bytes();
+    char *mem = ring_builtin_;
+    if (depth > 2 || !mem) {
+        if (cudaMallocHost(&ring_mem_, slot * depth) != cudaSuccess) {
+            ring_mem_ = nullptr;
+            return "device: pinned frame buffers could not be allocated";
         }
-        if (cudaEventCreateWithFlags(&step_done_, cudaEventDisableTiming) != cudaSuccess ||
-            cudaStreamCreateWithFlags(&st_copy_, cudaStreamNonBlocking) != cudaSuccess)
-            return "device: frame stream could not be created";
+        mem = static_cast<char *>(ring_mem_);
     }
+    for (int b = 0; b < 2; ++b) buf_used_[b] = false;
     ring_.resize(depth);
     for (int k = 0; k < depth; ++k) {
-        char *base = static_cast<char *>(ring_mem_) + slot * k;
+        char *base = mem + slot * k;
         Frame &f = ring_[k];
         f.x = reinterpret_cast<double *>(base);
         f.E = reinterpret_cast<long long *>(base + bx);

@@ -168,6 +168,9 @@ private:
     // spread/gather block.
     int tune_[3] = {0, 8, 128};
     std::string autotune();
+    // launch shapes tuned by an earlier context of the same shapes in this
+    // process: FFT z lines, columns, plane path, plane threads, PME threads
+    bool tune_lookup(int out[5]);
     std::string build_graph(double dt, int report);
     std::string build_graph_timed(double dt, int report);
     void free_graphs();
@@ -199,7 +202,9 @@ private:
         bool pending = false;
     };
     std::vector<Frame> ring_;
-    void *ring_mem_ = nullptr;  // one pinned block holding every slot
+    void *ring_mem_ = nullptr;        // pinned block of a ring deeper than two slots
+    char *ring_builtin_ = nullptr;    // two slots in the context's pinned block
+    size_t frame_slot_bytes() const;
     int ring_next_ = 0, ring_pending_ = 0;
     // Frame steps write their energies and positions into one of two device
     // buffers (A, B: report kinds 2, 3), alternately, so the copy of frame k
@@ -226,9 +231,13 @@ private:
     std::vector<double> energies_;  // [S][E_SLOTS] decoded
     long long *h_E_ = nullptr;       // pinned
     int *h_flags_ = nullptr;         // pinned
+    int *h_tail_ = nullptr;          // pinned: the exclusion build's totals
+    cudaEvent_t ev_setup_ = nullptr; // the set-up's point where those totals are in host memory
     int launches_per_step_ = 0, launches_per_rebuild_ = 0;
     template <typename T>
     T *dalloc(size_t n);
+    char *chunk(size_t bytes);
+    void arena_reserve(size_t bytes);
 };
 
 void launch_export(const DevView &v, int with_forces, cudaStream_t st);

@@ -45,7 +45,8 @@ struct FftPlan {
     FftSysDev *dsys = nullptr;
     std::vector<FftSysDev> hsys;
     FftWork *zwork = nullptr, *ywork = nullptr, *xwork = nullptr;
-    size_t cap[5] = {};   // allocated elements of dsys, zwork, ywork, xwork, pwork
+    void *buf = nullptr;  // one device buffer holding dsys and the work lists
+    size_t cap = 0;       // its bytes
     int nz = 0, ny = 0, nx = 0;
     int zlines = 16;    // real lines per block in the z passes (even)
     int cols = 8;       // z columns per block in the y and x passes
@@ -63,7 +64,8 @@ struct FftPlan {
     size_t smem_plane = 0;
 };
 
-void fft_plan_build(FftPlan &plan, int mixed);
+// Builds the plan; its device tables are copied in the order of stream st.
+void fft_plan_build(FftPlan &plan, int mixed, cudaStream_t st);
 void fft_plan_free(FftPlan &plan);
 // FFT kernel launches of one convolution with this plan.
 int fft_launch_count(const FftPlan &plan);
