@@ -727,19 +727,22 @@ void fft_plan_build(FftPlan &p, int mixed, cudaStream_t st) {
     const size_t bs = al(sizeof(FftSysDev) * std::max(p.S, 1)), bz = al(sizeof(FftWork) * (p.nz + 1)),
                  by = al(sizeof(FftWork) * (p.ny + 1)), bx = al(sizeof(FftWork) * (p.nx + 1)),
                  bp = al(sizeof(FftWork) * (p.npl + 1)), need = bs + bz + by + bx + bp;
-    if (need > p.cap || !p.buf) {
-        cudaFree(p.buf);
-        p.buf = nullptr;
-        p.cap = 0;
-        if (cudaMalloc(&p.buf, need) == cudaSuccess) p.cap = need;
+    char *b = static_cast<char *>(p.ext);
+    if (need > p.ext_cap || !p.ext) {
+        if (need > p.cap || !p.buf) {
+            cudaFree(p.buf);
+            p.buf = nullptr;
+            p.cap = 0;
+            if (cudaMalloc(&p.buf, need) == cudaSuccess) p.cap = need;
+        }
+        b = static_cast<char *>(p.buf);
     }
-    char *b = static_cast<char *>(p.buf);
     p.dsys = reinterpret_cast<FftSysDev *>(b);
     p.zwork = reinterpret_cast<FftWork *>(b + bs);
     p.ywork = reinterpret_cast<FftWork *>(b + bs + bz);
     p.xwork = reinterpret_cast<FftWork *>(b + bs + bz + by);
     p.pwork = reinterpret_cast<FftWork *>(b + bs + bz + by + bx);
-    if (p.buf) {
+    if (b) {
         // one copy from a host image of the buffer
         std::vector<char> img(need, 0);
         std::memcpy(img.data(), p.hsys.data(), sizeof(FftSysDev) * p.S);
@@ -747,12 +750,28 @@ void fft_plan_build(FftPlan &p, int mixed, cudaStream_t st) {
         std::memcpy(img.data() + bs + bz, y.data(), sizeof(FftWork) * p.ny);
         std::memcpy(img.data() + bs + bz + by, x.data(), sizeof(FftWork) * p.nx);
         std::memcpy(img.data() + bs + bz + by + bx, pl.data(), sizeof(FftWork) * p.npl);
-        cudaMemcpyAsync(p.buf, img.data(), need, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(b, img.data(), need, cudaMemcpyHostToDevice, st);
     }
     if (mixed)
         raise_all<float2, int, float>(p, 0);
     else
         raise_all<double2, double, double>(p, 8);
+}
+
+size_t fft_plan_bytes_max(const FftPlan &p) {
+    // the smallest blockings any build uses: 8 real lines per z block, 4 columns
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    size_t nz = 0, ny = 0, nx = 0, npl = 0;
+    for (int s = 0; s < p.S; ++s) {
+        const FftSysDev &F = p.hsys[s];
+        const int Kh = F.K[2] / 2 + 1, chunks = (Kh + 3) / 4;
+        nz += (F.K[0] * F.K[1] + 7) / 8;
+        ny += (size_t)F.K[0] * chunks;
+        nx += (size_t)F.K[1] * chunks;
+        npl += F.K[0];
+    }
+    return al(sizeof(FftSysDev) * std::max(p.S, 1)) + al(sizeof(FftWork) * (nz + 1)) +
+           al(sizeof(FftWork) * (ny + 1)) + al(sizeof(FftWork) * (nx + 1)) + al(sizeof(FftWork) * (npl + 1));
 }
 
 void fft_plan_free(FftPlan &p) {

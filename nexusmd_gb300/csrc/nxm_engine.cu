@@ -9,6 +9,7 @@
 // launches on one stream, everything resident on the device.
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -82,11 +83,47 @@ __global__ void k_state_to_slots(DevView v, const double *xyz, double *dx, doubl
     dz[s] = xyz[o + 2];
 }
 
+// Term ingest at context creation: term t of one kind (per = 2, 3 or 4
+// atoms; its system s found in the kind's per-system term offsets toff) has
+// its atom indices checked against the system's atom count and shifted by the
+// system's first atom, into int2 (per 2) or int4 (per 3, 4; unused word 0)
+// words.  An invalid term sets `errbit` in *err and takes the system's first
+// atom for every index, so later set-up kernels stay in range.  in and out may
+// be the same array when per is 2 or 4.
+__global__ void k_terms_ingest(const int *in, int per, int *out, int n, const int *toff, const int *first,
+                               const int *count, int S, int errbit, int *err) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int lo = 0, hi = S - 1;  // the last system whose terms start at or before t
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (toff[mid] <= t)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    int a[4] = {0, 0, 0, 0};
+    bool bad = false;
+    for (int k = 0; k < per; ++k) {
+        a[k] = in[(size_t)t * per + k];
+        bad |= a[k] < 0 || a[k] >= count[lo];
+    }
+    if (bad) atomicOr(err, errbit);
+    const int ow = per == 2 ? 2 : 4;
+    for (int k = 0; k < ow; ++k) out[(size_t)t * ow + k] = k < per ? first[lo] + (bad ? 0 : a[k]) : 0;
+}
+
 // FP32 copies of the bonded parameters (each double rounded once, as the
 // FP64 terms' values).
 __global__ void k_params_f32(const double2 *a, float2 *b, int n) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n) b[k] = make_float2((float)a[k].x, (float)a[k].y);
+}
+
+// The exceptions' (q_i q_j / 4 pi eps0, sigma, 4 eps) in FP32.
+__global__ void k_xc_params_f32(const double4 *a, float4 *b, int n) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) b[k] = make_float4((float)a[k].x, (float)a[k].y, (float)a[k].z, 0.f);
 }
 
 // ------------------------------------------------------------ host maths
@@ -146,9 +183,13 @@ static void bspline_moduli(int K, std::vector<double> &mod) {
     std::vector<double> bs(K + ORDER + 1, 0.0);
     for (int i = 1; i <= ORDER; i++) bs[i] = data[i - 1];
     mod.assign(K, 0.0);
+    // bs[j] is zero outside 1..ORDER, and the terms j < K it would add there
+    // are zeros that leave the sums' bits unchanged: the sums run over the
+    // non-zero terms only, in the same order
+    const int jmax = std::min(ORDER, K - 1);
     for (int i = 0; i < K; i++) {
         double sc = 0.0, ss = 0.0;
-        for (int j = 0; j < K; j++) {
+        for (int j = 1; j <= jmax; j++) {
             double arg = (2 * kPi * i * j) / K;
             sc += bs[j] * std::cos(arg);
             ss += bs[j] * std::sin(arg);
@@ -339,6 +380,26 @@ static void launch_influence(void *eterm, int mixed, long long coff, const doubl
 
 static size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 
+// Page-locked host memory: a page-aligned allocation registered with the
+// driver (for a few MB about ten times cheaper than cudaMallocHost here).
+static void *pinned_alloc(size_t b) {
+    b = (b + 65535) & ~(size_t)65535;
+    void *p = std::aligned_alloc(65536, b);
+    if (!p) return nullptr;
+    if (cudaHostRegister(p, b, cudaHostRegisterDefault) != cudaSuccess) {
+        cudaGetLastError();
+        std::free(p);
+        return nullptr;
+    }
+    return p;
+}
+
+static void pinned_free(void *p) {
+    if (!p) return;
+    cudaHostUnregister(p);
+    std::free(p);
+}
+
 static double now_ms() {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
@@ -397,7 +458,7 @@ Engine::~Engine() {
     free_graphs();
     for (void *p : allocs_) cudaFree(p);
     fft_plan_free(plan_);
-    if (h_E_) cudaFreeHost(h_E_);  // h_flags_, h_tail_ and the built-in frame ring lie in the same block
+    pinned_free(h_E_);  // h_flags_, h_tail_ and the built-in frame ring lie in the same block
     if (ev_fork_) cudaEventDestroy(ev_fork_);
     if (ev_join_) cudaEventDestroy(ev_join_);
     if (st_pme_) cudaStreamDestroy(st_pme_);
@@ -633,13 +694,12 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     cudaEventCreateWithFlags(&ev_join_, cudaEventDisableTiming);
     energies_.assign((size_t)S * E_SLOTS, 0.0);
     {
-        // pinned host memory in one block (pinning costs ~0.1 ms a call):
-        // the energy words, the flags, the exclusion build's totals and the
-        // default two-slot frame ring of nxm_step_async
+        // page-locked host memory in one block: the energy words, the
+        // flags, the exclusion build's totals and the default two-slot frame
+        // ring of nxm_step_async
         const size_t be = al256(sizeof(long long) * energies_.size()), bf = al256(sizeof(Flags)), bt = 256;
-        void *hp = nullptr;
-        if (cudaMallocHost(&hp, be + bf + bt + 2 * frame_slot_bytes()) != cudaSuccess)
-            return "device: pinned host allocation failed";
+        void *hp = pinned_alloc(be + bf + bt + 2 * frame_slot_bytes());
+        if (!hp) return "device: pinned host allocation failed";
         h_E_ = static_cast<long long *>(hp);
         h_flags_ = reinterpret_cast<int *>(static_cast<char *>(hp) + be);
         h_tail_ = reinterpret_cast<int *>(static_cast<char *>(hp) + be + bf);
@@ -752,15 +812,17 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st_);
         create_ms_[7] += now_ms() - t0;
     };
-    std::vector<int> sys_of(N_);
-    {
+    // each atom's system (one system: the zeroed array as it is)
+    std::vector<int> sys_of;
+    if (S > 1) {
+        sys_of.resize(N_);
         int o = 0;
         for (int s = 0; s < S; ++s) {
             std::fill(sys_of.begin() + o, sys_of.begin() + o + systems[s].n, s);
             o += systems[s].n;
         }
+        up(v_.sys_of, sys_of.data(), sizeof(int) * N_);
     }
-    up(v_.sys_of, sys_of.data(), sizeof(int) * N_);
     {
         std::vector<double> cat;
         auto atoms = [&](double *dst, const Span<double> HostSystem::*field) {
@@ -813,6 +875,112 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         up(v_.cgrid, cg.data(), sizeof(float2) * cg.size());
     }
 
+    // ---- bonds and terms (batch-global original indices).  Each kind's
+    // arrays go up as given -- one system's straight from the caller's
+    // array, several systems' concatenated with one host copy each -- and
+    // k_terms_ingest checks every atom index against its system's atom count
+    // and adds the system's first atom.  An invalid index is reported with
+    // the exclusion totals below.  Every bond feeds the exclusion sets; the
+    // bond, angle and torsion terms of a system come only with its force
+    // mask's bit.
+    int *ingest_err = dalloc<int>(1);
+    int2 *bonds_all = nullptr;
+    int nb_all = 0;
+    int *dtab = nullptr;  // [depth S][nonbonded on S][first atom S][atoms S][term offsets 4 x (S + 1)]
+    {
+        std::vector<int> tab(8 * (size_t)S + 4, 0);
+        int *depth = tab.data(), *nb_on = depth + S, *first = nb_on + S, *count = first + S;
+        int *o_all = count + S, *o_b = o_all + S + 1, *o_a = o_b + S + 1, *o_t = o_a + S + 1;
+        const unsigned bits[3] = {NXM_FORCE_BOND, NXM_FORCE_ANGLE, NXM_FORCE_TORSION};
+        int o = 0;
+        for (int s = 0; s < S; ++s) {
+            const HostSystem &h = systems[s];
+            depth[s] = h.excl_depth;
+            nb_on[s] = (h.force_mask & NXM_FORCE_NONBONDED) ? 1 : 0;
+            first[s] = o;
+            count[s] = h.n;
+            o += h.n;
+            const int m[3] = {(int)(h.bonds.size() / 2), (int)(h.angles.size() / 3), (int)(h.torsions.size() / 4)};
+            o_all[s + 1] = o_all[s] + m[0];
+            int *ok[3] = {o_b, o_a, o_t};
+            for (int k = 0; k < 3; ++k) ok[k][s + 1] = ok[k][s] + ((h.force_mask & bits[k]) ? m[k] : 0);
+        }
+        nb_all = o_all[S];
+        v_.nb = o_b[S];
+        v_.na = o_a[S];
+        v_.nt = o_t[S];
+        dtab = dalloc<int>(tab.size());
+        up(dtab, tab.data(), sizeof(int) * tab.size());
+        const int *d_first = dtab + 2 * S, *d_count = dtab + 3 * S, *d_oall = dtab + 4 * S,
+                  *d_ob = d_oall + S + 1, *d_oa = d_ob + S + 1, *d_ot = d_oa + S + 1;
+
+        // one field of the systems selected by `on`, concatenated in system order
+        std::vector<char> cat;
+        auto put = [&](void *dst, auto field, auto on) {
+            size_t bytes = 0;
+            int ns = 0, one = 0;
+            for (int s = 0; s < S; ++s) {
+                const auto &f = systems[s].*field;
+                if (on(s) && f.size()) {
+                    bytes += f.size() * sizeof(*f.data());
+                    ++ns;
+                    one = s;
+                }
+            }
+            if (!bytes) return;
+            if (ns == 1) {
+                up(dst, (systems[one].*field).data(), bytes);
+                return;
+            }
+            cat.resize(bytes);
+            size_t k = 0;
+            for (int s = 0; s < S; ++s) {
+                const auto &f = systems[s].*field;
+                if (on(s) && f.size()) {
+                    std::memcpy(cat.data() + k, f.data(), f.size() * sizeof(*f.data()));
+                    k += f.size() * sizeof(*f.data());
+                }
+            }
+            up(dst, cat.data(), bytes);
+        };
+        auto every = [](int) { return true; };
+        auto has = [&](unsigned bit) { return [&systems, bit](int s) { return (systems[s].force_mask & bit) != 0; }; };
+        auto ingest = [&](const void *in, int per, void *out, int n, const int *toff, int errbit) {
+            if (n > 0)
+                k_terms_ingest<<<(n + 255) / 256, 256, 0, st_>>>(static_cast<const int *>(in), per,
+                                                                 static_cast<int *>(out), n, toff, d_first, d_count,
+                                                                 S, errbit, ingest_err);
+        };
+        bonds_all = dalloc<int2>(nb_all);
+        put(bonds_all, &HostSystem::bonds, every);
+        ingest(bonds_all, 2, bonds_all, nb_all, d_oall, 1);
+        if (v_.nb == nb_all) {
+            v_.bond_orig = bonds_all;  // every system's bonds are terms too
+        } else {
+            v_.bond_orig = dalloc<int2>(v_.nb);
+            put(v_.bond_orig, &HostSystem::bonds, has(NXM_FORCE_BOND));
+            ingest(v_.bond_orig, 2, v_.bond_orig, v_.nb, d_ob, 1);
+        }
+        v_.bond_prm = dalloc<double2>(v_.nb);
+        put(v_.bond_prm, &HostSystem::bprm, has(NXM_FORCE_BOND));
+        int *araw = dalloc<int>(3 * (size_t)v_.na);
+        put(araw, &HostSystem::angles, has(NXM_FORCE_ANGLE));
+        v_.angle_orig = dalloc<int4>(v_.na);
+        ingest(araw, 3, v_.angle_orig, v_.na, d_oa, 2);
+        v_.angle_prm = dalloc<double2>(v_.na);
+        put(v_.angle_prm, &HostSystem::aprm, has(NXM_FORCE_ANGLE));
+        v_.tors_orig = dalloc<int4>(v_.nt);
+        put(v_.tors_orig, &HostSystem::torsions, has(NXM_FORCE_TORSION));
+        ingest(v_.tors_orig, 4, v_.tors_orig, v_.nt, d_ot, 4);
+        v_.tors_prm = dalloc<double2>(v_.nt);
+        put(v_.tors_prm, &HostSystem::tprm, has(NXM_FORCE_TORSION));
+        v_.tors_per = dalloc<int>(v_.nt);
+        put(v_.tors_per, &HostSystem::tper, has(NXM_FORCE_TORSION));
+        v_.bond_slot = dalloc<int2>(v_.nb);
+        v_.angle_slot = dalloc<int4>(v_.na);
+        v_.tors_slot = dalloc<int4>(v_.nt);
+    }
+
     // exclusion CSR (batch-global original indices) and the excluded pairs
     // j > i of the systems with the nonbonded force, built on the device
     // (k_exclusions_build.cu); a row too long for it: built on the host
@@ -820,42 +988,17 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     ExclBuild B{};
     {
         const double t0 = now_ms();
-        std::vector<int2> eb;  // every bond, batch-global (the search ignores the force mask)
-        std::vector<int> depth(S), nb_on(S);
-        {
-            size_t nbt = 0;
-            for (const HostSystem &h : systems) nbt += h.bonds.size() / 2;
-            eb.reserve(nbt);
-            int o = 0;
-            for (int s = 0; s < S; ++s) {
-                const HostSystem &h = systems[s];
-                for (size_t b = 0; b < h.bonds.size() / 2; ++b) {
-                    const int i = h.bonds[2 * b], j = h.bonds[2 * b + 1];
-                    if (i < 0 || j < 0 || i >= h.n || j >= h.n)
-                        return "createExclusions: Illegal particle index in list of bonds";
-                    eb.push_back(make_int2(o + i, o + j));
-                }
-                depth[s] = h.excl_depth;
-                nb_on[s] = (h.force_mask & NXM_FORCE_NONBONDED) ? 1 : 0;
-                o += h.n;
-            }
-        }
         v_.nxc = (int)xc_pairs.size();
         v_.xc_orig = dalloc<int2>(v_.nxc);
         if (v_.nxc) up(v_.xc_orig, xc_pairs.data(), sizeof(int2) * v_.nxc);
         B.n = N_;
-        B.nb = (int)eb.size();
+        B.nb = nb_all;
         B.nx = v_.nxc;
-        int2 *dbonds = dalloc<int2>(std::max<size_t>(eb.size(), 1));
-        if (!eb.empty()) up(dbonds, eb.data(), sizeof(int2) * eb.size());
-        B.bonds = dbonds;
+        B.bonds = bonds_all;
         B.xc = v_.xc_orig;
         B.sys_of = v_.sys_of;
-        int *tabs = dalloc<int>(2 * (size_t)S);
-        up(tabs, depth.data(), sizeof(int) * S);
-        up(tabs + S, nb_on.data(), sizeof(int) * S);
-        B.depth = tabs;
-        B.nb_on = tabs + S;
+        B.depth = dtab;
+        B.nb_on = dtab + S;
         int *w4 = dalloc<int>(4 * (size_t)N_);
         B.deg = w4;
         B.xdeg = w4 + N_;
@@ -863,7 +1006,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         B.xfill = w4 + 3 * (size_t)N_;
         B.aoff = dalloc<int>(N_ + 1);
         B.xoff = dalloc<int>(N_ + 1);
-        B.adj = dalloc<int>(std::max<size_t>(2 * eb.size(), 1));
+        B.adj = dalloc<int>(std::max<size_t>(2 * (size_t)nb_all, 1));
         B.xadj = dalloc<int>(std::max<size_t>(2 * xc_pairs.size(), 1));
         B.len = dalloc<int>(N_);
         B.plen = dalloc<int>(N_);
@@ -872,101 +1015,19 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         B.tile_sum = dalloc<int>(N_ / 4096 + 2);
         B.overflow = dalloc<int>(1);
         if (alloc_failed_) return "device allocation failed (exclusions)";
-        cudaMemsetAsync(B.overflow, 0, sizeof(int), st_);
         launch_exclusions_count(B, st_);
-        // the totals (list length, pair count, overflow) are read once the
-        // host has prepared the terms and the PME tables (below)
+        // the totals (list length, pair count, overflow) and the terms'
+        // index check are read once the host has prepared the PME tables
         cudaMemcpyAsync(h_tail_, B.eoff + N_, sizeof(int), cudaMemcpyDeviceToHost, st_);
         cudaMemcpyAsync(h_tail_ + 1, B.poff + N_, sizeof(int), cudaMemcpyDeviceToHost, st_);
         cudaMemcpyAsync(h_tail_ + 2, B.overflow, sizeof(int), cudaMemcpyDeviceToHost, st_);
+        cudaMemcpyAsync(h_tail_ + 3, ingest_err, sizeof(int), cudaMemcpyDeviceToHost, st_);
         cudaEventRecord(ev_setup_, st_);
         std::string e = check("exclusions");
         if (!e.empty()) return e;
         create_ms_[8] = now_ms() - t0;
     }
 
-    // terms (batch-global original indices); kinds disabled by the force mask
-    // get a zero count.  Sized once, parameters copied as given.
-    std::vector<int2> bo;
-    std::vector<double2> bp, ap, tp;
-    std::vector<int4> ao, to;
-    std::vector<int> tper;
-    {
-        size_t nb = 0, na = 0, nt = 0;
-        for (const HostSystem &h : systems) {
-            if (h.force_mask & NXM_FORCE_BOND) nb += h.bonds.size() / 2;
-            if (h.force_mask & NXM_FORCE_ANGLE) na += h.angles.size() / 3;
-            if (h.force_mask & NXM_FORCE_TORSION) nt += h.torsions.size() / 4;
-        }
-        bo.resize(nb);
-        bp.resize(nb);
-        ao.resize(na);
-        ap.resize(na);
-        to.resize(nt);
-        tp.resize(nt);
-        tper.resize(nt);
-        size_t kb = 0, ka = 0, kt = 0;
-        int o = 0;
-        for (const HostSystem &h : systems) {
-            for (int a : h.angles)
-                if (a < 0 || a >= h.n) return "angle atom index out of range";
-            for (int a : h.torsions)
-                if (a < 0 || a >= h.n) return "torsion atom index out of range";
-            if (h.force_mask & NXM_FORCE_BOND) {
-                const size_t m = h.bonds.size() / 2;
-                const int *b = h.bonds.data();
-                for (size_t k = 0; k < m; ++k) bo[kb + k] = make_int2(o + b[2 * k], o + b[2 * k + 1]);
-                if (m) std::memcpy(&bp[kb], h.bprm.data(), sizeof(double2) * m);
-                kb += m;
-            }
-            if (h.force_mask & NXM_FORCE_ANGLE) {
-                const size_t m = h.angles.size() / 3;
-                const int *a = h.angles.data();
-                for (size_t k = 0; k < m; ++k)
-                    ao[ka + k] = make_int4(o + a[3 * k], o + a[3 * k + 1], o + a[3 * k + 2], 0);
-                if (m) std::memcpy(&ap[ka], h.aprm.data(), sizeof(double2) * m);
-                ka += m;
-            }
-            if (h.force_mask & NXM_FORCE_TORSION) {
-                const size_t m = h.torsions.size() / 4;
-                const int *t = h.torsions.data();
-                for (size_t k = 0; k < m; ++k)
-                    to[kt + k] = make_int4(o + t[4 * k], o + t[4 * k + 1], o + t[4 * k + 2], o + t[4 * k + 3]);
-                if (m) {
-                    std::memcpy(&tp[kt], h.tprm.data(), sizeof(double2) * m);
-                    std::memcpy(&tper[kt], h.tper.data(), sizeof(int) * m);
-                }
-                kt += m;
-            }
-            o += h.n;
-        }
-    }
-    v_.nb = (int)bo.size();
-    v_.na = (int)ao.size();
-    v_.nt = (int)to.size();
-    v_.bond_orig = dalloc<int2>(v_.nb);
-    v_.bond_slot = dalloc<int2>(v_.nb);
-    v_.bond_prm = dalloc<double2>(v_.nb);
-    v_.angle_orig = dalloc<int4>(v_.na);
-    v_.angle_slot = dalloc<int4>(v_.na);
-    v_.angle_prm = dalloc<double2>(v_.na);
-    v_.tors_orig = dalloc<int4>(v_.nt);
-    v_.tors_slot = dalloc<int4>(v_.nt);
-    v_.tors_prm = dalloc<double2>(v_.nt);
-    v_.tors_per = dalloc<int>(v_.nt);
-    if (v_.nb) {
-        up(v_.bond_orig, bo.data(), sizeof(int2) * v_.nb);
-        up(v_.bond_prm, bp.data(), sizeof(double2) * v_.nb);
-    }
-    if (v_.na) {
-        up(v_.angle_orig, ao.data(), sizeof(int4) * v_.na);
-        up(v_.angle_prm, ap.data(), sizeof(double2) * v_.na);
-    }
-    if (v_.nt) {
-        up(v_.tors_orig, to.data(), sizeof(int4) * v_.nt);
-        up(v_.tors_prm, tp.data(), sizeof(double2) * v_.nt);
-        up(v_.tors_per, tper.data(), sizeof(int) * v_.nt);
-    }
     if (mixed_) {
         // the FP32 engine's parameters rounded once here rather than in
         // every evaluation (the same values: the kernels round the same doubles)
@@ -984,11 +1045,8 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     v_.xc_prm = dalloc<double4>(v_.nxc);
     if (v_.nxc) up(v_.xc_prm, xc_prm.data(), sizeof(double4) * v_.nxc);
     if (mixed_) {
-        std::vector<float4> xf(xc_prm.size());
-        for (size_t k = 0; k < xc_prm.size(); ++k)
-            xf[k] = make_float4((float)xc_prm[k].x, (float)xc_prm[k].y, (float)xc_prm[k].z, 0.f);
         v_.xc_prmf = dalloc<float4>(v_.nxc);
-        if (v_.nxc) up(v_.xc_prmf, xf.data(), sizeof(float4) * v_.nxc);
+        if (v_.nxc) k_xc_params_f32<<<(v_.nxc + 255) / 256, 256, 0, st_>>>(v_.xc_prm, v_.xc_prmf, v_.nxc);
     }
 
     // ---- PME
@@ -1058,6 +1116,8 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         // without them keep an empty grid that no block touches
         // launch shapes an earlier context of the same shapes tuned, else
         // the defaults until the autotuner has timed the candidates
+        plan_.ext_cap = fft_plan_bytes_max(plan_);
+        plan_.ext = dalloc<char>(plan_.ext_cap);
         tuned = opt.autotune && tune_lookup(tv);
         if (tuned) {
             plan_.zlines = tv[0];
@@ -1081,6 +1141,9 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         cudaEventSynchronize(ev_setup_);
         std::string e = check("exclusions");
         if (!e.empty()) return e;
+        if (h_tail_[3] & 1) return "createExclusions: Illegal particle index in list of bonds";
+        if (h_tail_[3] & 2) return "angle atom index out of range";
+        if (h_tail_[3] & 4) return "torsion atom index out of range";
         if (h_tail_[2]) {
             ex_on_host = true;
             int o = 0;
@@ -1096,7 +1159,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
             // exclusion correction pairs: only for systems with nonbonded enabled
             std::vector<int2> keep;
             for (auto &x : ex_pairs)
-                if (sysh_[sys_of[x.x]].force_mask & NXM_FORCE_NONBONDED) keep.push_back(x);
+                if (sysh_[S > 1 ? sys_of[x.x] : 0].force_mask & NXM_FORCE_NONBONDED) keep.push_back(x);
             ex_pairs.swap(keep);
             v_.nex = (int)ex_pairs.size();
             v_.ex_orig = dalloc<int2>(v_.nex);
@@ -1489,7 +1552,7 @@ void Engine::free_frames() {
         if (f.done) cudaEventSynchronize(f.done);
         if (f.done) cudaEventDestroy(f.done);
     }
-    if (ring_mem_) cudaFreeHost(ring_mem_);
+    pinned_free(ring_mem_);
     ring_mem_ = nullptr;
     ring_.clear();
     ring_next_ = ring_pending_ = 0;
@@ -1519,10 +1582,8 @@ std::string Engine::frames_init(int depth) {
                  slot = frame_slot_bytes();
     char *mem = ring_builtin_;
     if (depth > 2 || !mem) {
-        if (cudaMallocHost(&ring_mem_, slot * depth) != cudaSuccess) {
-            ring_mem_ = nullptr;
-            return "device: pinned frame buffers could not be allocated";
-        }
+        ring_mem_ = pinned_alloc(slot * depth);
+        if (!ring_mem_) return "device: pinned frame buffers could not be allocated";
         mem = static_cast<char *>(ring_mem_);
     }
     for (int b = 0; b < 2; ++b) buf_used_[b] = false;

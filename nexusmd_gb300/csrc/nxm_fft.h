@@ -47,6 +47,8 @@ struct FftPlan {
     FftWork *zwork = nullptr, *ywork = nullptr, *xwork = nullptr;
     void *buf = nullptr;  // one device buffer holding dsys and the work lists
     size_t cap = 0;       // its bytes
+    void *ext = nullptr;  // a buffer the caller owns, used instead where the tables fit
+    size_t ext_cap = 0;
     int nz = 0, ny = 0, nx = 0;
     int zlines = 16;    // real lines per block in the z passes (even)
     int cols = 8;       // z columns per block in the y and x passes
@@ -67,6 +69,9 @@ struct FftPlan {
 // Builds the plan; its device tables are copied in the order of stream st.
 void fft_plan_build(FftPlan &plan, int mixed, cudaStream_t st);
 void fft_plan_free(FftPlan &plan);
+// Bytes of the plan's device tables for any z and column blocking the
+// autotuner tries (hsys and S set).
+size_t fft_plan_bytes_max(const FftPlan &plan);
 // FFT kernel launches of one convolution with this plan.
 int fft_launch_count(const FftPlan &plan);
 // Shared memory of a line-path block: twiddles and two buffers of `lines`
