@@ -136,11 +136,13 @@ void nxm_default_options(nxm_options *opt);
 
 /* Create a context for n_systems systems; positions = all systems' atoms
  * concatenated [sum n][3].  Velocities start at zero (Initializer.cpp:18-24).
- * The caller's arrays are read before the call returns.  Unless the autotuner
- * times launch shapes (first context of its shapes in the process), the call
- * returns with the last set-up kernels still queued on the context's stream;
- * a device failure of theirs is reported by the next call that waits for the
- * device.  nxm_set_positions / nxm_set_velocities return likewise. */
+ * The caller's arrays are read before the call returns.  The call returns
+ * with the last set-up kernels and the first neighbour-list build still
+ * queued on the context's stream (the autotuner, when it times launch shapes
+ * for the first context of its shapes in the process, waits for the set-up
+ * before it); a device failure of theirs is reported by the next call that
+ * waits for the device.  nxm_set_positions / nxm_set_velocities likewise
+ * return once the caller's array is read. */
 int nxm_create(const nxm_system_desc *systems, int32_t n_systems, const nxm_options *opt,
                const double *positions, nxm_ctx **out);
 void nxm_destroy(nxm_ctx *ctx);

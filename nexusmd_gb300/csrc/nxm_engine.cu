@@ -26,12 +26,14 @@ namespace nxm {
 
 // ------------------------------------------------------------ rebuild gate
 
+// force 1: a rebuild in this step; 2: the context's first list, built
+// before any step (the interval then counts from the first step).
 __global__ void k_decide(DevView v, int force) {
     Flags *f = v.flags;
     int rb = force || f->since >= f->interval || f->skin_hit;
     f->rebuild = rb;
     f->skin_hit = 0;
-    f->since = rb ? 1 : f->since + 1;
+    f->since = rb ? (force == 2 ? 0 : 1) : f->since + 1;
     if (rb) f->nrebuild += 1;
 }
 
@@ -411,6 +413,20 @@ static double now_ms() {
 // chunk of its own above 8 MB.  Freed with the engine.
 constexpr size_t kArenaChunk = 32u << 20;
 
+// The compute stream, after the set-up's uploads and zeroing queued so far
+// on the copy stream.  The set-up uploads on the copy stream because an
+// upload from pageable memory returns only once every earlier operation of
+// its stream has run: on the compute stream each would wait for the
+// set-up's kernels.
+cudaStream_t Engine::kst() {
+    if (uploads_pending_) {
+        cudaEventRecord(ev_uploaded_, st_copy_);
+        cudaStreamWaitEvent(st_, ev_uploaded_, 0);
+        uploads_pending_ = false;
+    }
+    return st_;
+}
+
 char *Engine::chunk(size_t b) {
     const double t0 = now_ms();
     void *p = nullptr;
@@ -418,7 +434,10 @@ char *Engine::chunk(size_t b) {
         alloc_failed_ = true;
         return nullptr;
     }
-    cudaMemsetAsync(p, 0, b, st_);  // in the order of the set-up's work on the stream
+    // zeroed in the order of the set-up's uploads (copy stream), which the
+    // compute stream joins before its first kernel on them (kst)
+    cudaMemsetAsync(p, 0, b, st_copy_);
+    uploads_pending_ = true;
     allocs_.push_back(p);
     create_ms_[6] += now_ms() - t0;
     return static_cast<char *>(p);
@@ -453,12 +472,13 @@ Engine::~Engine() {
     for (int b = 0; b < 2; ++b)
         if (buf_free_[b]) cudaEventDestroy(buf_free_[b]);
     if (step_done_) cudaEventDestroy(step_done_);
-    if (ev_setup_) cudaEventDestroy(ev_setup_);
+    for (cudaEvent_t ev : {ev_setup_, ev_staged_, ev_stage_free_, ev_uploaded_})
+        if (ev) cudaEventDestroy(ev);
     if (st_copy_) cudaStreamDestroy(st_copy_);
     free_graphs();
     for (void *p : allocs_) cudaFree(p);
     fft_plan_free(plan_);
-    pinned_free(h_E_);  // h_flags_, h_tail_ and the built-in frame ring lie in the same block
+    pinned_free(h_E_);  // h_flags_ and h_tail_ lie in the same block
     if (ev_fork_) cudaEventDestroy(ev_fork_);
     if (ev_join_) cudaEventDestroy(ev_join_);
     if (st_pme_) cudaStreamDestroy(st_pme_);
@@ -502,6 +522,33 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     std::vector<int2> ex_pairs;
     std::vector<int2> xc_pairs;      // exception pairs, batch-global original indices
     std::vector<double4> xc_prm;
+    // Self energies (NonbondedForce.cpp:515-527), in the reference's serial
+    // order, on a helper thread while this one sets up the device (a chain
+    // of ~N dependent adds and N divisions); joined before init returns.
+    std::vector<double> self_e(S, 0.0);
+    struct Joiner {
+        std::thread t;
+        ~Joiner() {
+            if (t.joinable()) t.join();
+        }
+    } self_th;
+    {
+        bool big = false;
+        for (const HostSystem &h : systems) big |= h.n > 4096;
+        auto sum_self = [&systems, &self_e, S] {
+            for (int s = 0; s < S; ++s) {
+                const HostSystem &h = systems[s];
+                const double alpha = (1.0 / h.cutoff) * std::sqrt(-std::log(2.0 * h.tol));
+                double self = 0.0;
+                for (int i = 0; i < h.n; ++i) self -= kOne4PiEps0 * h.q[i] * h.q[i] * alpha / kSqrtPi;
+                self_e[s] = self;
+            }
+        };
+        if (big)
+            self_th.t = std::thread(sum_self);
+        else
+            sum_self();
+    }
     int off = 0, cell_off = 0, cg_total = 0;
     long long roff = 0, coff = 0;
     int tw_total = 0;
@@ -539,10 +586,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         H.atom_off = off;
         H.natoms = h.n;
         H.force_mask = h.force_mask;
-        // self energy (NonbondedForce.cpp:515-527)
-        double self = 0.0;
-        for (int i = 0; i < h.n; ++i) self -= kOne4PiEps0 * h.q[i] * h.q[i] * H.alpha / kSqrtPi;
-        H.self_energy = self;
+        H.self_energy = 0.0;  // summed by the helper thread below
 
         for (int d = 0; d < 3; ++d) {
             D.lb[d] = H.lb[d];
@@ -695,20 +739,23 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     energies_.assign((size_t)S * E_SLOTS, 0.0);
     {
         // page-locked host memory in one block: the energy words, the
-        // flags, the exclusion build's totals and the default two-slot frame
-        // ring of nxm_step_async
+        // flags and the exclusion build's totals (the frame ring of
+        // nxm_step_async comes with the first frame step, while the device
+        // builds the first list)
         const size_t be = al256(sizeof(long long) * energies_.size()), bf = al256(sizeof(Flags)), bt = 256;
-        void *hp = pinned_alloc(be + bf + bt + 2 * frame_slot_bytes());
+        void *hp = pinned_alloc(be + bf + bt);
         if (!hp) return "device: pinned host allocation failed";
         h_E_ = static_cast<long long *>(hp);
         h_flags_ = reinterpret_cast<int *>(static_cast<char *>(hp) + be);
         h_tail_ = reinterpret_cast<int *>(static_cast<char *>(hp) + be + bf);
-        ring_builtin_ = static_cast<char *>(hp) + be + bf + bt;
     }
     // the frame copies' stream and events
     for (int b = 0; b < 2; ++b) cudaEventCreateWithFlags(&buf_free_[b], cudaEventDisableTiming);
     cudaEventCreateWithFlags(&step_done_, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&ev_setup_, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&ev_staged_, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&ev_uploaded_, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&ev_stage_free_, cudaEventDisableTiming);
     cudaStreamCreateWithFlags(&st_copy_, cudaStreamNonBlocking);
     v_ = DevView{};
     v_.N = N_;
@@ -739,7 +786,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         arena_reserve(est);
     }
     SysDev *dsys = dalloc<SysDev>(S);
-    cudaMemcpyAsync(dsys, sysd_.data(), sizeof(SysDev) * S, cudaMemcpyHostToDevice, st_);
+    cudaMemcpyAsync(dsys, sysd_.data(), sizeof(SysDev) * S, cudaMemcpyHostToDevice, st_copy_);
     v_.sys = dsys;
     v_.sys_of = dalloc<int>(N_);
     v_.orig = dalloc<int>(N_);
@@ -790,7 +837,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         v_.groups = dalloc<CellGroup>(gr.size());
         v_.gspan = dalloc<int>(gr.size() * (size_t)kGroupSpanWords);
         v_.gspan_n = dalloc<int2>(gr.size());
-        cudaMemcpyAsync(v_.groups, gr.data(), sizeof(CellGroup) * gr.size(), cudaMemcpyHostToDevice, st_);
+        cudaMemcpyAsync(v_.groups, gr.data(), sizeof(CellGroup) * gr.size(), cudaMemcpyHostToDevice, st_copy_);
     }
     tiles_set_smem(hood_cap);
     v_.ncount = dalloc<int>(N_);
@@ -809,7 +856,8 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     // consumed
     auto up = [&](void *dst, const void *src, size_t bytes) {
         const double t0 = now_ms();
-        cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st_);
+        cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st_copy_);
+        uploads_pending_ = true;
         create_ms_[7] += now_ms() - t0;
     };
     // each atom's system (one system: the zeroed array as it is)
@@ -841,7 +889,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         atoms(v_.eps, &HostSystem::eps);
     }
     up(v_.tmp, positions, sizeof(double) * 3 * (size_t)N_);
-    launch_init_atoms(v_, v_.tmp, st_);
+    launch_init_atoms(v_, v_.tmp, kst());
 
     // cell-image displacement table: code ((ox+2)*5 + (oy+2))*12 + (oz+2) -> -(o . cs),
     // o relative to the first cell of a group (oz from -2 to kMaxGroupCells + 1)
@@ -947,7 +995,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         auto has = [&](unsigned bit) { return [&systems, bit](int s) { return (systems[s].force_mask & bit) != 0; }; };
         auto ingest = [&](const void *in, int per, void *out, int n, const int *toff, int errbit) {
             if (n > 0)
-                k_terms_ingest<<<(n + 255) / 256, 256, 0, st_>>>(static_cast<const int *>(in), per,
+                k_terms_ingest<<<(n + 255) / 256, 256, 0, kst()>>>(static_cast<const int *>(in), per,
                                                                  static_cast<int *>(out), n, toff, d_first, d_count,
                                                                  S, errbit, ingest_err);
         };
@@ -1015,7 +1063,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         B.tile_sum = dalloc<int>(N_ / 4096 + 2);
         B.overflow = dalloc<int>(1);
         if (alloc_failed_) return "device allocation failed (exclusions)";
-        launch_exclusions_count(B, st_);
+        launch_exclusions_count(B, kst());
         // the totals (list length, pair count, overflow) and the terms'
         // index check are read once the host has prepared the PME tables
         cudaMemcpyAsync(h_tail_, B.eoff + N_, sizeof(int), cudaMemcpyDeviceToHost, st_);
@@ -1039,14 +1087,14 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
             {v_.bond_prm, v_.bond_prmf}, {v_.angle_prm, v_.angle_prmf}, {v_.tors_prm, v_.tors_prmf}};
         const int cnt[3] = {v_.nb, v_.na, v_.nt};
         for (int k = 0; k < 3; ++k)
-            if (cnt[k]) k_params_f32<<<(cnt[k] + 255) / 256, 256, 0, st_>>>(pr[k].first, pr[k].second, cnt[k]);
+            if (cnt[k]) k_params_f32<<<(cnt[k] + 255) / 256, 256, 0, kst()>>>(pr[k].first, pr[k].second, cnt[k]);
     }
     v_.xc_slot = dalloc<int2>(v_.nxc);
     v_.xc_prm = dalloc<double4>(v_.nxc);
     if (v_.nxc) up(v_.xc_prm, xc_prm.data(), sizeof(double4) * v_.nxc);
     if (mixed_) {
         v_.xc_prmf = dalloc<float4>(v_.nxc);
-        if (v_.nxc) k_xc_params_f32<<<(v_.nxc + 255) / 256, 256, 0, st_>>>(v_.xc_prm, v_.xc_prmf, v_.nxc);
+        if (v_.nxc) k_xc_params_f32<<<(v_.nxc + 255) / 256, 256, 0, kst()>>>(v_.xc_prm, v_.xc_prmf, v_.nxc);
     }
 
     // ---- PME
@@ -1108,7 +1156,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         for (int s = 0; s < S; ++s) {
             const SysHost &H = sysh_[s];
             if (!(H.force_mask & NXM_FORCE_NONBONDED)) continue;
-            launch_influence(v_.eterm, mixed_, plan_.hsys[s].coff, dmod + mod_off[s], H.K, H.L, H.alpha, st_);
+            launch_influence(v_.eterm, mixed_, plan_.hsys[s].coff, dmod + mod_off[s], H.K, H.L, H.alpha, kst());
         }
         v_.pme_idx = dalloc<int4>(N_);
         v_.pme_frac = mixed_ ? (void *)dalloc<float4>(N_) : (void *)dalloc<double2>(2 * (size_t)N_);
@@ -1123,7 +1171,8 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
             plan_.zlines = tv[0];
             plan_.cols = tv[1];
         }
-        fft_plan_build(plan_, mixed_, st_);
+        fft_plan_build(plan_, mixed_, st_copy_);
+        uploads_pending_ = true;
         plan_.plane = tuned ? (tv[2] && plan_.plane_ok) : (plan_.plane_ok && fft_path_ == 2);
         if (tuned) plan_.plane_threads = tv[3];
         tune_[0] = plan_.plane ? 0 : plan_.zlines;
@@ -1170,7 +1219,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
             v_.nex = h_tail_[1];
             v_.ex_orig = dalloc<int2>(std::max(v_.nex, 1));
             if (alloc_failed_) return "device allocation failed (exclusions)";
-            launch_exclusions_fill(B, v_.excl_lst, v_.ex_orig, st_);
+            launch_exclusions_fill(B, v_.excl_lst, v_.ex_orig, kst());
         }
         v_.ex_slot = dalloc<int2>(v_.nex);
         create_ms_[8] += now_ms() - t0;
@@ -1187,6 +1236,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     v_.snap_x = dalloc<double>(3 * (size_t)N_);
     v_.snap_v = dalloc<double>(3 * (size_t)N_);
     v_.snap_f = dalloc<double>(3 * (size_t)N_);
+    stage3_ = dalloc<double>(3 * (size_t)N_);  // state uploads (set_positions, set_velocities)
     // frame steps' device buffers A and B (nxm_step_async)
     for (int b = 0; b < 2; ++b) {
         frame_x_[b] = dalloc<double>(3 * (size_t)N_);
@@ -1198,7 +1248,7 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
     v_.any_switch = 0;
     for (auto &d : sysd_) v_.any_switch |= d.use_switch ? 1 : 0;
     if (alloc_failed_) return "device allocation failed";
-    launch_derive_inputs(v_, st_);
+    launch_derive_inputs(v_, kst());
     force_rebuild_ = true;
     std::string e = check("set-up");
     if (!e.empty()) return e;
@@ -1215,6 +1265,14 @@ std::string Engine::init(const std::vector<HostSystem> &systems, const nxm_optio
         if (!e.empty()) return e;
         e = autotune();
     }
+    if (!e.empty()) return e;
+    if (self_th.t.joinable()) self_th.t.join();
+    for (int s = 0; s < S; ++s) sysh_[s].self_energy = self_e[s];
+    // the first neighbour list, built on the device while the caller goes on
+    launch_decide_rebuild(v_, 2, kst());
+    launch_nlist_rebuild(v_, st_);
+    force_rebuild_ = false;
+    e = check("first neighbour list");
     create_ms_[3] = now_ms() - t_rest;
     create_ms_[5] = create_ms_[0] + create_ms_[1] + create_ms_[2] + create_ms_[3];
     return e;
@@ -1350,23 +1408,34 @@ std::string Engine::autotune() {
     return check("autotune");
 }
 
+// A state array from the caller (original order, x y z per atom) into
+// slot order.  It goes up on the copy stream into a staging buffer -- an
+// upload from pageable memory returns once its source is consumed, and on
+// that stream it waits for no work queued on the compute stream -- and the
+// gather runs on the compute stream after it.  The staging buffer is written
+// again only after the last gather from it.
+std::string Engine::stage_state(const double *xyz, double *dx, double *dy, double *dz) {
+    if (stage_used_) cudaStreamWaitEvent(st_copy_, ev_stage_free_, 0);
+    cudaMemcpyAsync(stage3_, xyz, sizeof(double) * 3 * (size_t)N_, cudaMemcpyHostToDevice, st_copy_);
+    cudaEventRecord(ev_staged_, st_copy_);
+    cudaStreamWaitEvent(st_, ev_staged_, 0);
+    if (N_ > 0) k_state_to_slots<<<(N_ + 255) / 256, 256, 0, st_>>>(v_, stage3_, dx, dy, dz);
+    cudaEventRecord(ev_stage_free_, st_);
+    stage_used_ = true;
+    return check("state upload");
+}
+
 std::string Engine::set_positions(const double *xyz) {
-    // positions arrive in original order; the slot order is re-derived
-    // from them by the forced rebuild of the next evaluation
-    cudaMemcpyAsync(v_.tmp, xyz, sizeof(double) * 3 * (size_t)N_, cudaMemcpyHostToDevice, st_);
-    if (N_ > 0) k_state_to_slots<<<(N_ + 255) / 256, 256, 0, st_>>>(v_, v_.tmp, v_.x, v_.y, v_.z);
+    // the slot order is re-derived from the new positions by the forced
+    // rebuild of the next evaluation
+    std::string e = stage_state(xyz, v_.x, v_.y, v_.z);
+    if (!e.empty()) return e;
     launch_derive_inputs(v_, st_);
     force_rebuild_ = true;
     return check("set_positions");
 }
 
-// The caller's array is consumed when the upload returns (pageable memory is
-// staged); the gather runs in the stream's order before the next step.
-std::string Engine::set_velocities(const double *xyz) {
-    cudaMemcpyAsync(v_.tmp, xyz, sizeof(double) * 3 * (size_t)N_, cudaMemcpyHostToDevice, st_);
-    if (N_ > 0) k_state_to_slots<<<(N_ + 255) / 256, 256, 0, st_>>>(v_, v_.tmp, v_.vx, v_.vy, v_.vz);
-    return check("set_velocities");
-}
+std::string Engine::set_velocities(const double *xyz) { return stage_state(xyz, v_.vx, v_.vy, v_.vz); }
 
 // Force kernels of one evaluation (everything but the integrator).
 // Kernel launches of force_launches below, without launching.
@@ -1575,17 +1644,13 @@ std::string Engine::frames_init(int depth) {
     if (depth < 1 || depth > 64) return "frame ring depth must be 1..64";
     if (ring_pending_) return "frames still pending: wait for them first";
     free_frames();
-    // per slot the positions, the energy words and the flags, 256-byte
-    // aligned; two slots come with the context's pinned block, a deeper ring
-    // gets one pinned allocation of its own
+    // one page-locked block; per slot the positions, the energy words and
+    // the flags, 256-byte aligned
     const size_t bx = al256(sizeof(double) * 3 * (size_t)N_), be = al256(sizeof(long long) * energies_.size()),
                  slot = frame_slot_bytes();
-    char *mem = ring_builtin_;
-    if (depth > 2 || !mem) {
-        ring_mem_ = pinned_alloc(slot * depth);
-        if (!ring_mem_) return "device: pinned frame buffers could not be allocated";
-        mem = static_cast<char *>(ring_mem_);
-    }
+    ring_mem_ = pinned_alloc(slot * depth);
+    if (!ring_mem_) return "device: pinned frame buffers could not be allocated";
+    char *mem = static_cast<char *>(ring_mem_);
     for (int b = 0; b < 2; ++b) buf_used_[b] = false;
     ring_.resize(depth);
     for (int k = 0; k < depth; ++k) {

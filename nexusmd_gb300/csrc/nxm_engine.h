@@ -202,8 +202,7 @@ private:
         bool pending = false;
     };
     std::vector<Frame> ring_;
-    void *ring_mem_ = nullptr;        // pinned block of a ring deeper than two slots
-    char *ring_builtin_ = nullptr;    // two slots in the context's pinned block
+    void *ring_mem_ = nullptr;  // one page-locked block holding every slot
     size_t frame_slot_bytes() const;
     int ring_next_ = 0, ring_pending_ = 0;
     // Frame steps write their energies and positions into one of two device
@@ -233,10 +232,18 @@ private:
     int *h_flags_ = nullptr;         // pinned
     int *h_tail_ = nullptr;          // pinned: the exclusion build's totals
     cudaEvent_t ev_setup_ = nullptr; // the set-up's point where those totals are in host memory
+    // state uploads: staging buffer (3N doubles) and its events
+    double *stage3_ = nullptr;
+    cudaEvent_t ev_staged_ = nullptr, ev_stage_free_ = nullptr;
+    bool stage_used_ = false;
+    std::string stage_state(const double *xyz, double *dx, double *dy, double *dz);
     int launches_per_step_ = 0, launches_per_rebuild_ = 0;
     template <typename T>
     T *dalloc(size_t n);
     char *chunk(size_t bytes);
+    cudaStream_t kst();
+    bool uploads_pending_ = false;   // set-up uploads on the copy stream the compute stream has not joined
+    cudaEvent_t ev_uploaded_ = nullptr;
     void arena_reserve(size_t bytes);
 };
 
