@@ -64,16 +64,17 @@ __device__ __forceinline__ void load_dtab(const DevView &v, int sys, float4 *s_d
 }
 
 // Stage the group's neighbourhood (spans already in shared memory):
-// positions shifted into the group frame (.w = scaled charge in mixed mode),
-// LJ parameters (pair kernel), original indices (build).  Each atom's
+// positions shifted into the group frame, .w = the scaled charge (pair
+// kernel, mixed mode) or the original index's bits (build), and the LJ
+// parameters (pair kernel).  Each atom's
 // own-cell offset is shifted by its cell's displacement from the group's
 // first cell (a span's cells are consecutive in z, so the code is the
 // span's first code plus the z step).  In mixed mode each lane loads four
 // atoms of its span before it stores any, so the loads of a span are in
 // flight together.
 template <bool BUILD, bool MIXED>
-__device__ void stage(const DevView &v, const SysDev &S, float4 *s_q, float2 *s_lj, int *s_orig,
-                      const HoodSpan *spans, int nsp, const float4 *s_dt) {
+__device__ void stage(const DevView &v, const SysDev &S, float4 *s_q, float2 *s_lj, const HoodSpan *spans, int nsp,
+                      const float4 *s_dt) {
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int sp = warp; sp < nsp; sp += nw) {
         HoodSpan h = spans[sp];
@@ -102,11 +103,9 @@ __device__ void stage(const DevView &v, const SysDev &S, float4 *s_q, float2 *s_
                     if (t < h.count) {
                         int k = h.offset + t;
                         float4 D = s_dt[h.code0 + (((cj[u] >> 20) & 1023) - h.cz0)];
-                        s_q[k] = make_float4(p[u].x - D.x, p[u].y - D.y, p[u].z - D.z, p[u].w);
-                        if (BUILD)
-                            s_orig[k] = oj[u];
-                        else
-                            s_lj[k] = l[u];
+                        s_q[k] = make_float4(p[u].x - D.x, p[u].y - D.y, p[u].z - D.z,
+                                             BUILD ? __int_as_float(oj[u]) : p[u].w);
+                        if (!BUILD) s_lj[k] = l[u];
                     }
                 }
             }
@@ -117,8 +116,7 @@ __device__ void stage(const DevView &v, const SysDev &S, float4 *s_q, float2 *s_
                 float4 D = s_dt[h.code0 + (((cj >> 20) & 1023) - h.cz0)];
                 float o[3];
                 offset_in_cell(v, S, j, cj, o);
-                s_q[k] = make_float4(o[0] - D.x, o[1] - D.y, o[2] - D.z, 0.f);
-                if (BUILD) s_orig[k] = v.orig[j];
+                s_q[k] = make_float4(o[0] - D.x, o[1] - D.y, o[2] - D.z, BUILD ? __int_as_float(v.orig[j]) : 0.f);
             }
         }
     }
@@ -168,9 +166,8 @@ __global__ void __launch_bounds__(W * 32, W == kHoodWarps ? 2 : 1) k_build(DevVi
         return;
     }
     int cap = v.hood_cap;
-    float4 *s_q = reinterpret_cast<float4 *>(smem);
-    int *s_orig = reinterpret_cast<int *>(s_q + cap);
-    uint16_t *s_buf = reinterpret_cast<uint16_t *>(s_orig + cap);  // [W][2][256], 16-byte aligned
+    float4 *s_q = reinterpret_cast<float4 *>(smem);  // .w: the original index's bits
+    uint16_t *s_buf = reinterpret_cast<uint16_t *>(s_q + cap);  // [W][2][256], 16-byte aligned
     int *s_bnd = reinterpret_cast<int *>(s_buf + W * 512);
     HoodSpan *spans = reinterpret_cast<HoodSpan *>(s_bnd + 25 * (kRowCells + 1));
     int *s_n = reinterpret_cast<int *>(spans + kMaxSpans);
@@ -191,9 +188,9 @@ __global__ void __launch_bounds__(W * 32, W == kHoodWarps ? 2 : 1) k_build(DevVi
         return;
     }
     if (v.mixed)
-        stage<true, true>(v, S, s_q, nullptr, s_orig, spans, nsp, s_dt);
+        stage<true, true>(v, S, s_q, nullptr, spans, nsp, s_dt);
     else
-        stage<true, false>(v, S, s_q, nullptr, s_orig, spans, nsp, s_dt);
+        stage<true, false>(v, S, s_q, nullptr, spans, nsp, s_dt);
     int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     float rl2 = S.rlist2f * 1.0001f + 1e-6f;
     const float margin = 0.01f;
@@ -278,23 +275,23 @@ __global__ void __launch_bounds__(W * 32, W == kHoodWarps ? 2 : 1) k_build(DevVi
                 const int k = k0 + lane, kk = min(k, re - 1);
                 const float4 q = s_q[kk];
                 const float dx = pi3[0] - q.x, dy = pi3[1] - q.y, dz = pi3[2] - q.z;
-                const bool cand = (k < re) & (dx * dx + dy * dy + dz * dz < rl2) & (k != ki);
-                unsigned m = __ballot_sync(full, cand);
-                if (!m) continue;
-                const int oj = s_orig[kk];
+                bool cand = (k < re) & (dx * dx + dy * dy + dz * dz < rl2) & (k != ki);
+                const int oj = __float_as_int(q.w);
                 if (__any_sync(full, cand && (unsigned)(oj - ex_lo) <= ex_win)) {
                     bool ex = false;
                     for (int e = 0; e < nfast; ++e) ex |= (__shfl_sync(full, my_ex, e) == oj);
                     if (ne > 32 && cand)
                         for (int e = 32; e < ne; ++e) ex |= (v.excl_lst[e0 + e] == oj);
-                    m = __ballot_sync(full, cand && !ex);
+                    cand = cand && !ex;
                 }
+                const unsigned m = __ballot_sync(full, cand);
                 const int newc = count + __popc(m);
-                // every lane stores: a rejected candidate goes to newc + lane,
-                // past the entries so far -- a slot that a later entry
-                // overwrites or that lies beyond the list's count (never in
-                // the half being stored: at most 32 entries come per iteration)
-                buf[(((m >> lane) & 1u) ? count + __popc(m & lt) : newc + lane) & 511] = (uint16_t)(k << kEntryShift);
+                // every lane stores: a rejected candidate goes to count + 32 +
+                // lane, past the entries of this iteration -- a slot that a
+                // later entry overwrites or that lies beyond the list's count
+                // (never in the half being stored: at most 32 entries come
+                // per iteration)
+                buf[(cand ? count + __popc(m & lt) : count + 32 + lane) & 511] = (uint16_t)(k << kEntryShift);
                 if ((newc ^ count) >> 8) {
                     // chunk count >> 8 complete: one 16-byte store per lane
                     __syncwarp();
@@ -468,7 +465,7 @@ __global__ void __launch_bounds__(W * 32, W == kHoodWarps ? 2 : 1) k_pairs_mixed
         if (threadIdx.x == 0) atomicOr(&v.flags->error, ERR_NLIST_OVERFLOW);
         return;
     }
-    stage<false, true>(v, S, s_q, s_lj, nullptr, spans, nsp, s_dt);
+    stage<false, true>(v, S, s_q, s_lj, spans, nsp, s_dt);
     int czf = (c3f >> 20) & 1023;
     const float lo = S.cut2f_lo, hi = S.cut2f_hi;
     const PairPrm P{S.ex2c, S.a04, S.k2a, S.sw_distf, S.cutofff, S.use_switch};
@@ -702,7 +699,7 @@ __global__ void k_collect(DevView v, int sys_sel, int *out, long long cap, unsig
 
 static size_t tail_bytes() { return kMaxSpans * sizeof(HoodSpan) + 4 * sizeof(int); }
 static size_t smem_build(int cap, int warps) {
-    return (size_t)cap * (sizeof(float4) + sizeof(int)) + (size_t)warps * 512 * sizeof(uint16_t) +
+    return (size_t)cap * sizeof(float4) + (size_t)warps * 512 * sizeof(uint16_t) +
            25 * (kRowCells + 1) * sizeof(int) + tail_bytes();
 }
 static size_t smem_pairs(int cap, int mixed) {
