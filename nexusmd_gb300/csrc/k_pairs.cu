@@ -201,22 +201,17 @@ __global__ void __launch_bounds__(W * 32, W == kHoodWarps ? 2 : 1) k_build(DevVi
     for (int i = a0 + warp; i < a1; i += nw) {
         float pi3[3];
         i_in_group_frame(v, S, i, czf, pi3);
-        // i's own tile index: row (0, 0), cell oz_i counted from the
-        // neighbourhood's anchor cell (the group's first non-empty cell)
-        int c3i = v.cell3[i];
-        int cz_i = (c3i >> 20) & 1023;
-        int oz_i = hood_wrap(cz_i - czf, S.nc[2]);
-        int key_i = S.cell_off + ((c3i & 1023) * S.nc[1] + ((c3i >> 10) & 1023)) * S.nc[2] + cz_i;
-        int ki = s_bnd[12 * (kRowCells + 1) + oz_i + 2] + (i - v.cell_start[key_i]);
         int oi = v.orig[i];
         int e0 = v.excl_off[oi];
         int ne = v.excl_off[oi + 1] - e0;
         int my_ex = lane < ne ? v.excl_lst[e0 + lane] : -1;
         int nfast = ne < 32 ? ne : 32;
-        // index window of the exclusion partners [ex_lo, ex_lo + ex_win]:
-        // candidates outside it need no membership test (none without exclusions)
-        const int ex_lo = ne ? v.excl_lst[e0] : -1;
-        const unsigned ex_win = ne ? (unsigned)(v.excl_lst[e0 + ne - 1] - ex_lo) : 0u;
+        // Index window [ex_lo, ex_lo + ex_win] of i itself and its exclusion
+        // partners (rows ascending): a candidate outside it needs no
+        // membership test.  i is left out by its index too, so every image
+        // of i is (the far one lies beyond the list radius anyway).
+        const int ex_lo = ne ? min(v.excl_lst[e0], oi) : oi;
+        const unsigned ex_win = (unsigned)((ne ? max(v.excl_lst[e0 + ne - 1], oi) : oi) - ex_lo);
         int count = 0;
         uint16_t *out = v.nl16 + (size_t)i * v.stride;
         // lane r < 25: the tile range [kb, ke) of row r that i's sphere reaches
@@ -272,13 +267,16 @@ __global__ void __launch_bounds__(W * 32, W == kHoodWarps ? 2 : 1) k_build(DevVi
             rows &= rows - 1;
             const int rb = __shfl_sync(full, kb, r), re = __shfl_sync(full, ke, r);
             for (int k0 = rb; k0 < re; k0 += 32) {
-                const int k = k0 + lane, kk = min(k, re - 1);
-                const float4 q = s_q[kk];
+                // k past the row's end reads a later row or the chunk
+                // buffers behind the tile, inside the block's shared
+                // memory; such a lane is no candidate
+                const int k = k0 + lane;
+                const float4 q = s_q[k];
                 const float dx = pi3[0] - q.x, dy = pi3[1] - q.y, dz = pi3[2] - q.z;
-                bool cand = (k < re) & (dx * dx + dy * dy + dz * dz < rl2) & (k != ki);
+                bool cand = (k < re) & (fmaf(dz, dz, fmaf(dy, dy, dx * dx)) < rl2);
                 const int oj = __float_as_int(q.w);
                 if (__any_sync(full, cand && (unsigned)(oj - ex_lo) <= ex_win)) {
-                    bool ex = false;
+                    bool ex = oj == oi;
                     for (int e = 0; e < nfast; ++e) ex |= (__shfl_sync(full, my_ex, e) == oj);
                     if (ne > 32 && cand)
                         for (int e = 32; e < ne; ++e) ex |= (v.excl_lst[e0 + e] == oj);
