@@ -145,7 +145,8 @@ class Engine:
                  force_mask=FORCE_ALL, box="reference", grid=None, use_switch=0,
                  switch_dist=0.0, exclusion_depth=3, max_neighbors=0, device=0, exceptions=False,
                  fft_path=0, autotune=True):
-        """``box``: "reference" (extent + 1%, as the reference) or "explicit"
+        """``force_mask``: one mask for every system, or a sequence with one
+        per system; ``box``: "reference" (extent + 1%, as the reference) or "explicit"
         (each system's periodic box [0, L)); ``grid``: None = each system's
         ``grid`` attribute, (0,0,0) = the reference's power-of-two rule;
         ``exceptions``: pass each system's ``exc_idx`` / ``exc_prm`` exception
@@ -160,7 +161,10 @@ class Engine:
         self._keep = []
         descs = (SystemDesc * len(systems))()
         pos = []
-        for d, s in zip(descs, systems):
+        masks = list(force_mask) if isinstance(force_mask, (list, tuple)) else [force_mask] * len(systems)
+        if len(masks) != len(systems):
+            raise ValueError("one force mask per system")
+        for d, s, mask in zip(descs, systems, masks):
             k = dict(m=_arr(s.mass, np.float64), q=_arr(s.charge, np.float64),
                      sg=_arr(s.sigma, np.float64), ep=_arr(s.epsilon, np.float64),
                      ba=_arr(s.bonds, np.int32), bp=_arr(s.bond_prm, np.float64),
@@ -186,7 +190,7 @@ class Engine:
                 d.box_from_positions = 0
                 for i in range(3):
                     d.box_lb[i], d.box_ub[i] = 0.0, float(s.box[i])
-            d.force_mask = int(force_mask)
+            d.force_mask = int(mask)
             d.exclusion_depth = int(exclusion_depth)
             if exceptions and getattr(s, "exc_idx", None) is not None and len(s.exc_idx):
                 k["xi"] = _arr(s.exc_idx, np.int32)

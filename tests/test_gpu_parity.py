@@ -265,6 +265,36 @@ def test_batched_uneven_systems_match_per_system_oracle(oracle):
         eng.close()
 
 
+def test_batch_with_per_system_force_masks_matches_oracle(oracle):
+    """Systems of one batch with different force masks: each kind's terms
+    are taken in for the systems whose mask has it (the bonds of every
+    system still define its exclusions), so the per-system term offsets
+    have empty ranges between full ones; each system's FP64 forces and
+    energies equal the oracle's with that system's mask."""
+    systems = [sy.with_exceptions(x) for x in sy.batch_systems(count=4, seed=91, lo=2000, hi=5000)]
+    masks = [15, 8, 13, 3]  # all; nonbonded only; no angles; bonds + angles only
+    eng = _engine(systems, precision=0, skin=0.1, rebuild_interval=10, box="explicit", exceptions=True,
+                  force_mask=masks)
+    F = eng.compute_forces()
+    off = 0
+    for k, (s, m) in enumerate(zip(systems, masks)):
+        lb, ub = np.zeros(3), s.box.copy()
+        box = oracle.box_explicit(lb, ub)
+        eo, el = oracle.exclusions(s.n, s.bonds)
+        xc = (s.exc_idx, s.exc_prm) if m & 8 else None
+        if xc is not None:
+            eo, el = oracle.union_exclusions(eo, el, s.exc_idx)
+        d = oracle.describe(s, force_mask=m, box_mode=1, lb=lb, ub=ub, exceptions=xc)
+        F0, E0 = oracle.forces(d, s.pos, box, eo, el)
+        assert rel_rms(F[off:off + s.n], F0) <= 1e-9, (k, m, rel_rms(F[off:off + s.n], F0))
+        E = eng.energies(k)
+        scale = max(abs(E0[t]) for t in TERMS) or 1.0
+        for t in TERMS:
+            assert abs(E[t] - E0[t]) <= 1e-9 * scale + 1e-6, (k, m, t, E[t], E0[t])
+        off += s.n
+    eng.close()
+
+
 def test_contexts_of_different_sizes_coexist():
     """Per-kernel launch limits are process-wide: a context created after a
     larger one must not make the larger one's launches fail."""
